@@ -1,0 +1,339 @@
+"""Benchmark: line-point gradient evaluations per second on one GB300.
+
+Workload (the gather-roofline configuration): a periodic line of L = 2^20
+points on a 2^20 x 1024 pinning field (Gaussian-filtered white noise,
+correlation length xi = 4 cells, unit variance, seed 5, grid spacing 1). A
+step evaluates the gradient of 8 independent line instances (h = band centre
++ a smooth random walk of std 8 cells; the 8 lines sit in 8 disjoint row
+bands), so every step touches ~8x the per-instance footprint, more than twice
+the 129 MB L2: inputs larger than L2, no flush needed.
+
+Reports (one JSON line on rank 0): value = points/s with inputs resident in
+HBM; e2e = the same through the host-buffer C-ABI call (qew_gradient_host,
+pinned host buffers, copies inside the timed region); roofline of the
+dominant gradient kernel against the measured HBM copy bandwidth;
+cpu_baseline = the CPU oracle's OpenMP gradient on the machine's host cores.
+
+``--impl reference`` times the CPU implementation of the path (the oracle's
+restatement of the reference, OpenMP on all host cores) on the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "line-point gradient evals/s"
+UNIT = "points/s"
+L_FULL, NY_FULL, XI, SEED, N_INST = 1 << 20, 1024, 4.0, 5, 8
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32split"])
+    ap.add_argument("--small", action="store_true",
+                    help="small case for profiling: L=2^20, 64-row field, one instance")
+    ap.add_argument("--profile-run", action="store_true",
+                    help="GPU timed loop only (no e2e, CPU baseline or clock sampling)")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- helpers
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def smooth_walk(rng, n, std, corr):
+    """A smooth periodic random line: Gaussian-filtered white noise, given std."""
+    w = rng.standard_normal(n)
+    k = np.fft.rfftfreq(n)
+    f = np.fft.irfft(np.fft.rfft(w) * np.exp(-0.5 * (2 * np.pi * corr * k) ** 2), n)
+    return f * (std / f.std())
+
+
+def gaussian_field_gpu(torch, nx, ny, xi, seed):
+    """Seeded white noise, Gaussian filter exp(-(2 pi xi f)^2/2) (f in cycles
+    per cell) applied axis by axis in Fourier space, unit population std.
+    Layout (nx, ny), y fastest (the reference's host layout)."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    w = torch.randn((nx, ny), dtype=torch.float64, device="cuda", generator=g)
+    ky = torch.fft.rfftfreq(ny, device="cuda", dtype=torch.float64)
+    w = torch.fft.irfft(torch.fft.rfft(w, dim=1) * torch.exp(-0.5 * (2 * math.pi * xi * ky) ** 2),
+                        n=ny, dim=1)
+    kx = torch.fft.rfftfreq(nx, device="cuda", dtype=torch.float64)[:, None]
+    w = torch.fft.irfft(torch.fft.rfft(w, dim=0) * torch.exp(-0.5 * (2 * math.pi * xi * kx) ** 2),
+                        n=nx, dim=0)
+    w -= w.mean()
+    w /= w.std(unbiased=False)
+    return w.contiguous()
+
+
+# ---------------------------------------------------------- reference arm
+def cpu_gradient_rate(seconds: float, L: int = L_FULL, ny: int = 64):
+    """The CPU oracle's OpenMP gradient on a bounded sample: a 2^20-point line
+    on a 2^20 x 64 field. The raw synthetic field serves as the coefficient
+    array (the gather's cost does not depend on the values)."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(SEED)
+    coef = rng.standard_normal((L, ny))
+    f = O.BSplineField(coef, float(L), float(ny), coef=coef)
+    h = ny / 2 + smooth_walk(rng, L, 8.0, 64.0)
+    p = O.params(float(L), 1.0, 0.0, 0)
+    out = np.empty(L)
+    O.gradient(h, p, f, omp=True, out=out)  # warm
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        O.gradient(h, p, f, omp=True, out=out)
+        reps += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": reps * L / dt, "unit": UNIT, "cores": O.omp_max_threads(), "kind": "port",
+            "sample": "%d gradient evals of a 2^20-point line on a 2^20x%d FP64 field "
+                      "(OpenMP, %.1f s)" % (reps, ny, dt)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+    rng = np.random.default_rng(SEED)
+    L, ny = L_FULL, 64
+    coef = rng.standard_normal((L, ny))
+    f = O.BSplineField(coef, float(L), float(ny), coef=coef)
+    h = ny / 2 + smooth_walk(rng, L, 8.0, 64.0)
+    p = O.params(float(L), 1.0, 0.0, 0)
+    out = np.empty(L)
+    for _ in range(max(args.warmup, 0)):
+        O.gradient(h, p, f, omp=True, out=out)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.gradient(h, p, f, omp=True, out=out)
+    dt = time.perf_counter() - t0
+    val = args.steps * L / dt
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "gradient of a 2^20-point line, FP64, CPU oracle (reference "
+                                   "algorithm restated), 2^20x64-row sample field",
+                       "L": L, "rows": ny},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": O.omp_max_threads(),
+                             "kind": "port",
+                             "sample": "one 2^20-point gradient per step, OpenMP"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from qew_gb300 import build as qbuild
+    qbuild.build()
+    import qew_gb300 as Q
+
+    prec = Q.QEW_PREC_FP64 if args.precision == "fp64" else Q.QEW_PREC_FP32_SPLIT
+    if args.small:
+        L, ny, n_inst = L_FULL, 64, 1
+    else:
+        L, ny, n_inst = L_FULL, NY_FULL, N_INST
+    store = Q.QEW_STORE_FP64 | (Q.QEW_STORE_FP32 if prec == Q.QEW_PREC_FP32_SPLIT else 0)
+    field = gaussian_field_gpu(torch, L, ny, XI, SEED + rank)
+    noise = Q.FilteredNoise(field, float(L), float(ny), store=store)
+    del field
+    torch.cuda.empty_cache()
+    rng = np.random.default_rng(SEED + 1000 * rank)
+    band = ny / n_inst
+    hs_host = [np.ascontiguousarray(band * (k + 0.5) + smooth_walk(rng, L, min(8.0, band / 8), 64.0))
+               for k in range(n_inst)]
+    hs = [torch.as_tensor(h, device="cuda") for h in hs_host]
+    gs = [torch.empty_like(h) for h in hs]
+    p = Q.Params(float(L), 1.0, 0.0, Q.Model.Linear)
+    ctx = noise.ctx
+
+    def step():
+        for k in range(n_inst):
+            Q.gradient(hs[k], p, noise, gs[k], precision=prec)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    if not args.profile_run:
+        clocks.start()
+        time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launches() - l0
+    t_ms = e0.elapsed_time(e1)
+    if ws > 1:
+        t = torch.tensor([t_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_ms = float(t.item())
+        torch.distributed.barrier()
+    clk = clocks.stop() if not args.profile_run else None
+    points = args.steps * n_inst * L
+    value = ws * points / (t_ms * 1e-3)
+
+    # roofline of the dominant kernel (the only kernel in the timed region)
+    bytes_per_point = 48.0 if prec == Q.QEW_PREC_FP64 else 32.0
+    launch_ms = t_ms / max(launches, 1)
+    achieved = bytes_per_point * L / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": None,
+            "kernel": "k_gradient" if prec == Q.QEW_PREC_FP64 else "k_gradient_split",
+            "bytes_per_point": bytes_per_point, "peak_source": peak_kind}
+
+    e2e = None
+    cpu = None
+    if not args.profile_run:
+        # end to end through the C ABI with pinned host buffers
+        hh = [torch.as_tensor(h).pin_memory().numpy() for h in hs_host]
+        gh = [torch.empty(L, dtype=torch.float64).pin_memory().numpy() for _ in range(n_inst)]
+        for k in range(n_inst):
+            Q.gradient_host(hh[k], p, noise, gh[k], precision=prec)
+        torch.cuda.synchronize()
+        e2e_steps = max(2, args.steps // 2)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            for k in range(n_inst):
+                Q.gradient_host(hh[k], p, noise, gh[k], precision=prec)
+        dt = time.perf_counter() - t0
+        e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
+               "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8}
+        if rank == 0 and args.cpu_seconds > 0:
+            cpu = cpu_gradient_rate(args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": max(args.warmup, 3),
+                "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if prec == Q.QEW_PREC_FP64 else "f32",
+                "data": "synthetic",
+                "config": {"workload": "gradient of %d line instances of L=2^20 points on a "
+                                       "2^20x%d field (xi=4 cells), %s gather"
+                                       % (n_inst, ny, args.precision),
+                           "L": L, "rows": ny, "instances_per_step": n_inst,
+                           "model": "linear", "l2": "inputs larger than L2 (8 disjoint row "
+                                                   "bands per step)",
+                           "parallelism": "replicas" if ws > 1 else "single GPU"},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+                "gpu_launches": launches, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

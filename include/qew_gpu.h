@@ -1,0 +1,260 @@
+/*
+ * qew_gpu.h -- C ABI of the GB300-native qEW hot path.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, status codes; no C++ or
+ * torch types. Each entry point names the reference interface it replaces
+ * (IMTEK-Simulation/qEW, paths relative to its source tree).
+ *
+ * Conventions
+ *  - Device pointers (d_*) are caller-owned allocations on the context's
+ *    device; host pointers (h_*) are ordinary or pinned host memory.
+ *  - Work is enqueued on the context's CUDA stream (default: the legacy
+ *    default stream, so it orders with other work there). Functions that
+ *    return a host value (a scalar, a result struct) synchronise that stream
+ *    before returning; the pure device-to-device kernels (gradient, sample,
+ *    Langevin step) return as soon as their work is enqueued, like a Kokkos
+ *    parallel_for.
+ *  - A context is not thread-safe; use one per host thread.
+ *  - Errors come back as a qew_status; qew_last_error() has the message.
+ *    Where the reference throws (rk_block on odd n) the ABI returns
+ *    QEW_ERR_ODD_LENGTH instead.
+ *  - Every device-side wait is bounded and reports QEW_ERR_TIMEOUT.
+ */
+#ifndef QEW_GPU_H
+#define QEW_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    QEW_OK = 0,
+    QEW_ERR_INVALID = 1,     /* bad argument (size, null pointer, kind) */
+    QEW_ERR_ODD_LENGTH = 2,  /* rk_block on odd n (rosso_krauth.h:134-136) */
+    QEW_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+    QEW_ERR_NOMEM = 4,       /* device allocation failed */
+    QEW_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    QEW_ERR_UNSUPPORTED = 6  /* valid request this build does not handle */
+} qew_status;
+
+typedef struct qew_ctx qew_ctx;
+typedef struct qew_field qew_field;
+typedef struct qew_langevin qew_langevin;
+
+/* Model, qew_model.h:20 */
+enum { QEW_MODEL_LINEAR = 0, QEW_MODEL_ARCLENGTH = 1 };
+
+/* Params, qew_model.h:22-27. dx = physical_size / n. */
+typedef struct {
+    double physical_size;
+    double line_tension;
+    double driving_force;
+    int model;
+} qew_params;
+
+/* Field kinds. QEW_FIELD_BSPLINE is FilteredNoise / DeviceNoise
+ * (filtered_noise.h:67-210). The analytic kinds are the Noise functors the
+ * reference's own tests inject, so those known-answer tests run unchanged:
+ *   ZERO       ZeroNoise                       (test_lbfgs.cpp:24-27)
+ *   CONST      ConstNoise{v0=p0}               (test_qew_model.cpp:38-42)
+ *   HARMONIC   HarmonicWell{k=p0, y0=p1}       (test_lbfgs.cpp:30-38)
+ *   WASHBOARD  SinusoidNoise{A=p0, k=p1}       (test_rosso_krauth.cpp:24-31)
+ *   SINCOS     AnalyticNoise{amp=p0,kx=p1,ky=p2} (test_qew_model.cpp:22-34) */
+enum {
+    QEW_FIELD_BSPLINE = 0,
+    QEW_FIELD_ZERO = 1,
+    QEW_FIELD_CONST = 2,
+    QEW_FIELD_HARMONIC = 3,
+    QEW_FIELD_WASHBOARD = 4,
+    QEW_FIELD_SINCOS = 5
+};
+
+/* Storage flags for B-spline fields. */
+enum { QEW_STORE_FP64 = 1, QEW_STORE_FP32 = 2 };
+
+/* Precision of the gather in the model kernels. FP64 is the drop-in (parity)
+ * form; FP32_SPLIT gathers an FP32 coefficient copy at a height split into
+ * an integer cell plus an FP32 fraction, accumulating in FP64. */
+enum { QEW_PREC_FP64 = 0, QEW_PREC_FP32_SPLIT = 1 };
+
+/* LbfgsParams, lbfgs.h:32-52 (same fields, same defaults). */
+typedef struct {
+    int m;
+    double ftol;
+    int max_iter;
+    double c1;
+    double ls_shrink;
+    int max_ls;
+    double curvature_eps;
+    int precondition;
+    double precond_shift;
+} qew_lbfgs_params;
+
+/* LbfgsResult, lbfgs.h:54-61 */
+typedef struct {
+    int iterations;
+    double max_force;
+    int converged;
+    long n_func_evals;
+    long n_curvature_skips;
+    long n_ls_restarts;
+} qew_lbfgs_result;
+
+/* RkParams, rosso_krauth.h:34-41 */
+typedef struct {
+    double dstep;
+    double max_advance;
+    double root_tol;
+    double sweep_tol;
+    double runaway;
+    int max_sweeps;
+} qew_rk_params;
+
+/* RkResult, rosso_krauth.h:43-49 */
+typedef struct {
+    int blocked;
+    int runaway;
+    int sweeps;
+    double total_advance;
+    double mean_h;
+} qew_rk_result;
+
+/* L-BFGS solver forms. PLAIN is the reference's host-driven loop, one
+ * kernel (and, for each reduction, one device->host read) per vector
+ * operation, with a cuFFT preconditioner: the one-line-per-launch comparator.
+ * RESIDENT runs the whole solve in one persistent kernel (device-side
+ * two-loop, shared-memory FFT preconditioner, Armijo search, history ring). */
+enum { QEW_LBFGS_PLAIN = 0, QEW_LBFGS_RESIDENT = 1 };
+
+/* ---------------------------------------------------------------- context */
+const char *qew_status_string(qew_status s);
+qew_status qew_ctx_create(int device, qew_ctx **out);
+qew_status qew_ctx_destroy(qew_ctx *ctx);
+/* cuda_stream is a cudaStream_t (NULL = legacy default stream). */
+qew_status qew_ctx_set_stream(qew_ctx *ctx, void *cuda_stream);
+qew_status qew_ctx_synchronize(qew_ctx *ctx);
+const char *qew_last_error(const qew_ctx *ctx);
+/* Number of this library's kernels launched through ctx so far. */
+uint64_t qew_ctx_launch_count(const qew_ctx *ctx);
+
+/* ------------------------------------------------------------------ field */
+/* FilteredNoise(const real_t *field, nx, ny, Lx, Ly), filtered_noise.h:189 /
+ * filtered_noise.cpp:84-90 + build_coefficients (filtered_noise.cpp:92-136).
+ * h_field is the reference's host layout, row-major [nx][ny] (i*ny + j).
+ * The periodic cubic B-spline prefilter runs on the device; coefficients are
+ * stored x-fastest ([ny][nx]) in FP64 and/or FP32 per store_flags. */
+qew_status qew_field_create_from_host(qew_ctx *ctx, const double *h_field,
+                                      int nx, int ny, double Lx, double Ly,
+                                      int store_flags, qew_field **out);
+/* Same, from a field already on the device (d_field, layout [nx][ny]). */
+qew_status qew_field_create_from_device(qew_ctx *ctx, const double *d_field,
+                                        int nx, int ny, double Lx, double Ly,
+                                        int store_flags, qew_field **out);
+/* Analytic potentials (see the kind enum). */
+qew_status qew_field_create_analytic(qew_ctx *ctx, int kind, double p0,
+                                     double p1, double p2, qew_field **out);
+qew_status qew_field_destroy(qew_field *field);
+/* Download the FP64 coefficients in the reference's host layout [nx][ny]. */
+qew_status qew_field_get_coefficients(qew_ctx *ctx, const qew_field *field,
+                                      double *h_coef);
+/* DeviceNoise::sample at m points (filtered_noise.h:103-134); any of the
+ * outputs may be NULL. */
+qew_status qew_field_sample(qew_ctx *ctx, const qew_field *field,
+                            const double *d_x, const double *d_y, int m,
+                            double *d_v, double *d_dvdx, double *d_dvdy);
+
+/* ------------------------------------------------------------------ model */
+/* objective(h, p, noise), qew_model.h:102-109. Deterministic reduction. */
+qew_status qew_objective(qew_ctx *ctx, const qew_field *field,
+                         const double *d_h, int n, const qew_params *p,
+                         double *h_out);
+/* objective(x0, d, alpha, p, noise), qew_model.h:112-119. */
+qew_status qew_objective_trial(qew_ctx *ctx, const qew_field *field,
+                               const double *d_x0, const double *d_d,
+                               double alpha, int n, const qew_params *p,
+                               double *h_out);
+/* gradient(h, p, noise, grad[, ws]), qew_model.h:149-201, fused into one
+ * kernel (edge pass and per-site combine share one launch). */
+qew_status qew_gradient(qew_ctx *ctx, const qew_field *field,
+                        const double *d_h, int n, const qew_params *p,
+                        double *d_grad);
+/* gradient with the gather precision selectable (QEW_PREC_*). */
+qew_status qew_gradient_prec(qew_ctx *ctx, const qew_field *field,
+                             const double *d_h, int n, const qew_params *p,
+                             int precision, double *d_grad);
+/* Host-buffer gradient: copies h_h to the device, runs the gradient and
+ * copies the result back into h_grad, all on the context's stream; returns
+ * after the copy back has completed. */
+qew_status qew_gradient_host(qew_ctx *ctx, const qew_field *field,
+                             const double *h_h, int n, const qew_params *p,
+                             int precision, double *h_grad);
+
+/* ----------------------------------------------------------------- L-BFGS */
+qew_status qew_lbfgs_default_params(qew_lbfgs_params *lp);
+/* lbfgs_minimize(h, p, noise, lp), lbfgs.h:94-287; relaxes d_h in place. */
+qew_status qew_lbfgs_minimize(qew_ctx *ctx, const qew_field *field,
+                              double *d_h, int n, const qew_params *p,
+                              const qew_lbfgs_params *lp,
+                              qew_lbfgs_result *res);
+/* Same with the solver form chosen explicitly (QEW_LBFGS_*). */
+qew_status qew_lbfgs_minimize_form(qew_ctx *ctx, const qew_field *field,
+                                   double *d_h, int n, const qew_params *p,
+                                   const qew_lbfgs_params *lp, int form,
+                                   qew_lbfgs_result *res);
+/* The preconditioner alone, d = M^{-1} q (lbfgs.h:116-146, 173-180), with
+ * the shift rule of lbfgs.h:131-135 (shift <= 0 selects the auto shift). */
+qew_status qew_precond_apply(qew_ctx *ctx, const double *d_q, int n,
+                             double line_tension, double physical_size,
+                             double shift, int form, double *d_out);
+
+/* --------------------------------------------------------------- Langevin */
+/* LangevinDynamics(n, seed), dynamics.h:31-32. Increments are N(0,1) from a
+ * Philox4x32-10 counter stream keyed by seed, counter (site pair, step). */
+qew_status qew_langevin_create(qew_ctx *ctx, int n, uint64_t seed,
+                               qew_langevin **out);
+qew_status qew_langevin_destroy(qew_langevin *lgv);
+/* LangevinDynamics::step(h, p, noise, drift, diff), dynamics.h:34-64:
+ * h_i += -drift * dE/dh_i + diff * xi_i (xi only when diff > 0). */
+qew_status qew_langevin_step(qew_langevin *lgv, const qew_field *field,
+                             double *d_h, const qew_params *p, double drift,
+                             double diff);
+/* Same step with caller-supplied increments d_xi[n] (trajectory parity). */
+qew_status qew_langevin_step_increments(qew_langevin *lgv,
+                                        const qew_field *field, double *d_h,
+                                        const qew_params *p, double drift,
+                                        double diff, const double *d_xi);
+/* The increments the next qew_langevin_step would use, without stepping. */
+qew_status qew_langevin_peek_increments(qew_langevin *lgv, double *d_xi);
+/* Steps taken so far (the Philox step counter). */
+uint64_t qew_langevin_steps(const qew_langevin *lgv);
+
+/* ---------------------------------------------------------- Rosso-Krauth */
+/* rk_site_velocity (rosso_krauth.h:51-82) of every site of d_h. */
+qew_status qew_rk_site_velocity(qew_ctx *ctx, const qew_field *field,
+                                const double *d_h, int n, const qew_params *p,
+                                double *d_vel);
+/* rk_block(h, p, noise, rp), rosso_krauth.h:128-194; advances d_h in place.
+ * Odd n returns QEW_ERR_ODD_LENGTH (the reference throws). */
+qew_status qew_rk_block(qew_ctx *ctx, const qew_field *field, double *d_h,
+                        int n, const qew_params *p, const qew_rk_params *rp,
+                        qew_rk_result *res);
+/* Force bisection for f_c (no reference counterpart; the reference ramps,
+ * qew_runs.h:226-241): from a blocked d_h at f_lo and an unblocked f_hi,
+ * bisect f, restarting each rk_block from the last blocked configuration,
+ * until (f_hi - f_lo) <= rtol * f_hi. d_h ends as the blocked configuration
+ * at f_lo; *f_c = (f_lo + f_hi) / 2. */
+qew_status qew_depinning_bisect(qew_ctx *ctx, const qew_field *field,
+                                double *d_h, int n, const qew_params *p,
+                                const qew_rk_params *rp, double f_lo,
+                                double f_hi, double rtol, int max_steps,
+                                double *f_c, double *f_lo_out,
+                                double *f_hi_out, int *n_blocks);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QEW_GPU_H */

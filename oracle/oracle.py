@@ -1,0 +1,271 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module, and only as the checker. The product
+(``qew_gb300``) never imports it and has no CPU fallback.
+
+Arrays are numpy float64. Fields use the reference's host layout
+``field[i, j]`` with i the x (column) index and j the y (row) index.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field as dc_field
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+D = C.c_double
+I = C.c_int
+PD = C.POINTER(C.c_double)
+
+
+class QoNoise(C.Structure):
+    _fields_ = [("kind", I), ("coef", PD), ("nx", I), ("ny", I), ("dx", D),
+                ("dy", D), ("p0", D), ("p1", D), ("p2", D)]
+
+
+class QoParams(C.Structure):
+    _fields_ = [("physical_size", D), ("line_tension", D),
+                ("driving_force", D), ("model", I)]
+
+
+class QoLbfgsParams(C.Structure):
+    _fields_ = [("m", I), ("ftol", D), ("max_iter", I), ("c1", D),
+                ("ls_shrink", D), ("max_ls", I), ("curvature_eps", D),
+                ("precondition", I), ("precond_shift", D)]
+
+
+class QoLbfgsResult(C.Structure):
+    _fields_ = [("iterations", I), ("max_force", D), ("converged", I),
+                ("n_func_evals", C.c_long), ("n_curvature_skips", C.c_long),
+                ("n_ls_restarts", C.c_long)]
+
+
+class QoRkParams(C.Structure):
+    _fields_ = [("dstep", D), ("max_advance", D), ("root_tol", D),
+                ("sweep_tol", D), ("runaway", D), ("max_sweeps", I)]
+
+
+class QoRkResult(C.Structure):
+    _fields_ = [("blocked", I), ("runaway", I), ("sweeps", I),
+                ("total_advance", D), ("mean_h", D)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        L = _lib
+        L.qo_sample_many.argtypes = [C.POINTER(QoNoise), PD, PD, I, PD, PD, PD]
+        L.qo_prefilter.argtypes = [PD, I, I, PD]
+        L.qo_prefilter.restype = I
+        L.qo_fft.argtypes = [PD, PD, I, I]
+        L.qo_rfft.argtypes = [PD, I, PD, PD]
+        L.qo_irfft.argtypes = [PD, PD, I, PD]
+        for fn in ("qo_objective", "qo_objective_omp"):
+            getattr(L, fn).argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise)]
+            getattr(L, fn).restype = D
+        L.qo_objective_trial.argtypes = [PD, PD, D, I, C.POINTER(QoParams), C.POINTER(QoNoise)]
+        L.qo_objective_trial.restype = D
+        for fn in ("qo_gradient", "qo_gradient_omp"):
+            getattr(L, fn).argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise), PD]
+        L.qo_omp_max_threads.restype = I
+        L.qo_lbfgs_default_params.argtypes = [C.POINTER(QoLbfgsParams)]
+        L.qo_lbfgs_minimize.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
+                                        C.POINTER(QoLbfgsParams), C.POINTER(QoLbfgsResult)]
+        L.qo_precond_apply.argtypes = [PD, I, D, D, D, PD]
+        L.qo_langevin_step.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
+                                       D, D, PD, PD]
+        L.qo_rk_site_velocity.argtypes = [I, I, D, D, D, I, D, D, D, C.POINTER(QoNoise)]
+        L.qo_rk_site_velocity.restype = D
+        L.qo_rk_block.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
+                                  C.POINTER(QoRkParams), C.POINTER(QoRkResult)]
+        L.qo_rk_block.restype = I
+        L.qo_depinning_bisect.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
+                                          C.POINTER(QoRkParams), D, D, D, I,
+                                          PD, PD, PD, C.POINTER(I)]
+        L.qo_depinning_bisect.restype = I
+        L.qo_philox_normals.argtypes = [C.c_uint64, C.c_uint64, I, PD]
+    return _lib
+
+
+def _p(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(PD)
+
+
+# --------------------------------------------------------------------------
+# Noise descriptors (the production field and the reference tests' stubs)
+# --------------------------------------------------------------------------
+class Noise:
+    """Base: holds a QoNoise struct (and keeps the coefficient array alive)."""
+
+    def __init__(self, kind: int, p0=0.0, p1=0.0, p2=0.0):
+        self.s = QoNoise(kind, None, 0, 0, 1.0, 1.0, p0, p1, p2)
+        self._keep = None
+
+
+class BSplineField(Noise):
+    """FilteredNoise(field, nx, ny, Lx, Ly), filtered_noise.cpp:84-90."""
+
+    def __init__(self, field_xy: np.ndarray, Lx: float, Ly: float,
+                 coef: np.ndarray | None = None):
+        field_xy = np.ascontiguousarray(field_xy, dtype=np.float64)
+        nx, ny = field_xy.shape
+        super().__init__(0)
+        if coef is None:
+            coef = prefilter(field_xy)
+        self.field = field_xy
+        self.coef = np.ascontiguousarray(coef, dtype=np.float64)
+        self.nx, self.ny, self.Lx, self.Ly = nx, ny, Lx, Ly
+        self.s.coef = _p(self.coef)
+        self.s.nx, self.s.ny = nx, ny
+        self.s.dx, self.s.dy = Lx / nx, Ly / ny
+        self._keep = self.coef
+
+
+def ZeroNoise():
+    return Noise(1)
+
+
+def ConstNoise(v0):
+    return Noise(2, v0)
+
+
+def HarmonicWell(k=2.0, y0=0.5):
+    return Noise(3, k, y0)
+
+
+def SinusoidNoise(A=0.1, k=2.0 * 3.14159265358979323846):
+    return Noise(4, A, k)
+
+
+def AnalyticNoise(amp=0.3, kx=0.7, ky=1.3):
+    return Noise(5, amp, kx, ky)
+
+
+def prefilter(field_xy: np.ndarray) -> np.ndarray:
+    field_xy = np.ascontiguousarray(field_xy, dtype=np.float64)
+    nx, ny = field_xy.shape
+    coef = np.empty_like(field_xy)
+    rc = lib().qo_prefilter(_p(field_xy), nx, ny, _p(coef))
+    assert rc == 0
+    return coef
+
+
+def sample(noise: Noise, x: np.ndarray, y: np.ndarray):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    m = x.size
+    v, dx, dy = np.empty(m), np.empty(m), np.empty(m)
+    lib().qo_sample_many(C.byref(noise.s), _p(x), _p(y), m, _p(v), _p(dx), _p(dy))
+    return v, dx, dy
+
+
+# --------------------------------------------------------------------------
+# Model / solvers
+# --------------------------------------------------------------------------
+def params(physical_size=1.0, line_tension=1.0, driving_force=0.0, model=0):
+    return QoParams(physical_size, line_tension, driving_force, int(model))
+
+
+def objective(h, p: QoParams, noise: Noise, omp=False) -> float:
+    h = np.ascontiguousarray(h, dtype=np.float64)
+    fn = lib().qo_objective_omp if omp else lib().qo_objective
+    return fn(_p(h), h.size, C.byref(p), C.byref(noise.s))
+
+
+def objective_trial(x0, d, alpha, p: QoParams, noise: Noise) -> float:
+    x0 = np.ascontiguousarray(x0, dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    return lib().qo_objective_trial(_p(x0), _p(d), alpha, x0.size, C.byref(p), C.byref(noise.s))
+
+
+def gradient(h, p: QoParams, noise: Noise, omp=False, out=None) -> np.ndarray:
+    h = np.ascontiguousarray(h, dtype=np.float64)
+    g = np.empty_like(h) if out is None else out
+    fn = lib().qo_gradient_omp if omp else lib().qo_gradient
+    fn(_p(h), h.size, C.byref(p), C.byref(noise.s), _p(g))
+    return g
+
+
+def omp_max_threads() -> int:
+    return lib().qo_omp_max_threads()
+
+
+def lbfgs_default_params(**kw) -> QoLbfgsParams:
+    lp = QoLbfgsParams()
+    lib().qo_lbfgs_default_params(C.byref(lp))
+    for k, v in kw.items():
+        setattr(lp, k, v)
+    return lp
+
+
+def lbfgs_minimize(h: np.ndarray, p: QoParams, noise: Noise, lp: QoLbfgsParams):
+    """Relaxes h in place (numpy float64); returns a QoLbfgsResult."""
+    assert h.dtype == np.float64 and h.flags["C_CONTIGUOUS"]
+    res = QoLbfgsResult()
+    lib().qo_lbfgs_minimize(_p(h), h.size, C.byref(p), C.byref(noise.s), C.byref(lp), C.byref(res))
+    return res
+
+
+def precond_apply(q, kappa, physical_size, shift) -> np.ndarray:
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    d = np.empty_like(q)
+    lib().qo_precond_apply(_p(q), q.size, kappa, physical_size, shift, _p(d))
+    return d
+
+
+def langevin_step(h: np.ndarray, p: QoParams, noise: Noise, drift, diff, xi):
+    xi = np.ascontiguousarray(xi, dtype=np.float64)
+    g = np.empty_like(h)
+    lib().qo_langevin_step(_p(h), h.size, C.byref(p), C.byref(noise.s), drift, diff, _p(xi), _p(g))
+
+
+def rk_params(dstep=0.0, max_advance=0.0, root_tol=1e-10, sweep_tol=1e-9,
+              runaway=0.0, max_sweeps=200000) -> QoRkParams:
+    return QoRkParams(dstep, max_advance, root_tol, sweep_tol, runaway, max_sweeps)
+
+
+def rk_site_velocity(i, n, dx, lt, f, model, hi, hl, hr, noise: Noise) -> float:
+    return lib().qo_rk_site_velocity(i, n, dx, lt, f, model, hi, hl, hr, C.byref(noise.s))
+
+
+def rk_block(h: np.ndarray, p: QoParams, noise: Noise, rp: QoRkParams):
+    assert h.dtype == np.float64 and h.flags["C_CONTIGUOUS"]
+    res = QoRkResult()
+    rc = lib().qo_rk_block(_p(h), h.size, C.byref(p), C.byref(noise.s), C.byref(rp), C.byref(res))
+    if rc != 0:
+        raise ValueError("rk_block: line length must be even for the red-black sweep")
+    return res
+
+
+def depinning_bisect(h: np.ndarray, p: QoParams, noise: Noise, rp: QoRkParams,
+                     f_lo, f_hi, rtol=1e-10, max_steps=200):
+    fc, flo, fhi = D(), D(), D()
+    nb = I()
+    rc = lib().qo_depinning_bisect(_p(h), h.size, C.byref(p), C.byref(noise.s), C.byref(rp),
+                                   f_lo, f_hi, rtol, max_steps, C.byref(fc), C.byref(flo),
+                                   C.byref(fhi), C.byref(nb))
+    if rc != 0:
+        raise ValueError("depinning_bisect: line length must be even")
+    return fc.value, flo.value, fhi.value, nb.value
+
+
+def philox_normals(seed: int, step: int, n: int) -> np.ndarray:
+    out = np.empty(n)
+    lib().qo_philox_normals(seed, step, n, _p(out))
+    return out
+
+
+def fft(re, im, inverse=False):
+    re = np.array(re, dtype=np.float64)
+    im = np.array(im, dtype=np.float64)
+    lib().qo_fft(_p(re), _p(im), re.size, 1 if inverse else 0)
+    return re, im

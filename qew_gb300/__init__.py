@@ -1,0 +1,456 @@
+"""qew_gb300 -- GB300-native hot path of the quenched Edwards-Wilkinson line.
+
+Python mirror of the reference's operator API (IMTEK-Simulation/qEW,
+src/qew_model.h, src/filtered_noise.h, src/lbfgs.h, src/dynamics.h,
+src/rosso_krauth.h) over the C ABI of ``include/qew_gpu.h``. Lines are CUDA
+float64 torch tensors (torch supplies device memory and streams only); all
+arithmetic runs in this package's own sm_103a kernels. Names, argument
+meaning, defaults and error behaviour follow the reference:
+
+=========================================  ====================================
+reference                                  here
+=========================================  ====================================
+``Params``, ``Model``                      :class:`Params`, :class:`Model`
+``FilteredNoise(field, nx, ny, Lx, Ly)``   :class:`FilteredNoise`
+test stubs (ZeroNoise, HarmonicWell, ...)  :func:`ZeroNoise` etc.
+``objective(h, p, noise)``                 :func:`objective`
+``objective(x0, d, alpha, p, noise)``      :func:`objective_trial`
+``gradient(h, p, noise, grad)``            :func:`gradient`
+``lbfgs_minimize(h, p, noise, lp)``        :func:`lbfgs_minimize`
+``LangevinDynamics(n, seed).step(...)``    :class:`LangevinDynamics`
+``rk_site_velocity`` / ``rk_block``        :func:`rk_site_velocity`, :func:`rk_block`
+=========================================  ====================================
+
+``rk_block`` raises ``ValueError`` on an odd line length where the reference
+throws ``std::invalid_argument``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass, fields
+
+import numpy as np
+
+from . import _capi
+from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # noqa: F401
+                    QEW_FIELD_SINCOS, QEW_FIELD_WASHBOARD, QEW_FIELD_ZERO,
+                    QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT, QEW_PREC_FP32_SPLIT,
+                    QEW_PREC_FP64, QEW_STORE_FP32, QEW_STORE_FP64, QewError)
+
+__all__ = [
+    "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
+    "SinusoidNoise", "AnalyticNoise", "objective", "objective_trial", "gradient",
+    "gradient_host", "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "precond_apply",
+    "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
+    "depinning_bisect", "Context", "default_context", "QewError",
+]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+class Model(enum.IntEnum):  # qew_model.h:20
+    Linear = 0
+    Arclength = 1
+
+
+@dataclass
+class Params:  # qew_model.h:22-27
+    physical_size: float = 1.0
+    line_tension: float = 1.0
+    driving_force: float = 0.0
+    model: Model = Model.Linear
+
+    def c(self) -> _capi.qew_params:
+        return _capi.qew_params(float(self.physical_size), float(self.line_tension),
+                                float(self.driving_force), int(self.model))
+
+
+@dataclass
+class LbfgsParams:  # lbfgs.h:32-52
+    m: int = 8
+    ftol: float = 1e-6
+    max_iter: int = 10000
+    c1: float = 1e-4
+    ls_shrink: float = 0.5
+    max_ls: int = 30
+    curvature_eps: float = 1e-12
+    precondition: bool = False
+    precond_shift: float = 0.0
+
+    def c(self) -> _capi.qew_lbfgs_params:
+        return _capi.qew_lbfgs_params(int(self.m), float(self.ftol), int(self.max_iter),
+                                      float(self.c1), float(self.ls_shrink), int(self.max_ls),
+                                      float(self.curvature_eps), int(bool(self.precondition)),
+                                      float(self.precond_shift))
+
+
+@dataclass
+class LbfgsResult:  # lbfgs.h:54-61
+    iterations: int = 0
+    max_force: float = 0.0
+    converged: bool = False
+    n_func_evals: int = 0
+    n_curvature_skips: int = 0
+    n_ls_restarts: int = 0
+
+
+@dataclass
+class RkParams:  # rosso_krauth.h:34-41
+    dstep: float = 0.0
+    max_advance: float = 0.0
+    root_tol: float = 1e-10
+    sweep_tol: float = 1e-9
+    runaway: float = 0.0
+    max_sweeps: int = 200000
+
+    def c(self) -> _capi.qew_rk_params:
+        return _capi.qew_rk_params(float(self.dstep), float(self.max_advance),
+                                   float(self.root_tol), float(self.sweep_tol),
+                                   float(self.runaway), int(self.max_sweeps))
+
+
+@dataclass
+class RkResult:  # rosso_krauth.h:43-49
+    blocked: bool = False
+    runaway: bool = False
+    sweeps: int = 0
+    total_advance: float = 0.0
+    mean_h: float = 0.0
+
+
+# ---------------------------------------------------------------- context
+class Context:
+    """One qew_ctx (device, stream, reduction and workspace arenas)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _capi.load()
+        self.device = device
+        h = C.c_void_p()
+        _capi.check(self.lib.qew_ctx_create(device, C.byref(h)), None, "qew_ctx_create")
+        self.h = h
+
+    def sync_stream(self):
+        """Run subsequent work on torch's current stream of this device."""
+        torch = _torch()
+        s = torch.cuda.current_stream(self.device).cuda_stream
+        self.lib.qew_ctx_set_stream(self.h, C.c_void_p(s))
+
+    def launches(self) -> int:
+        return int(self.lib.qew_ctx_launch_count(self.h))
+
+    def synchronize(self):
+        _capi.check(self.lib.qew_ctx_synchronize(self.h), self.h, "synchronize")
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.qew_ctx_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+_contexts: dict[int, Context] = {}
+
+
+def default_context(device: int | None = None) -> Context:
+    torch = _torch()
+    if device is None:
+        device = torch.cuda.current_device()
+    ctx = _contexts.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        _contexts[device] = ctx
+    ctx.sync_stream()
+    return ctx
+
+
+def _ptr(t) -> C.c_void_p:
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise ValueError("expected a CUDA tensor")
+    if t.dtype != torch.float64 or not t.is_contiguous():
+        raise ValueError("expected a contiguous float64 CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+# ------------------------------------------------------------------ noise
+class _Noise:
+    kind: int = -1
+
+    def __init__(self):
+        self.h = None
+        self.ctx = None
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.lib.qew_field_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class FilteredNoise(_Noise):
+    """FilteredNoise(field, nx, ny, Lx, Ly) (filtered_noise.h:183-189).
+
+    ``field`` is the real-space field in the reference's host layout
+    ``field[i, j]`` (i along x, j along y), as a numpy array or a CUDA tensor.
+    The periodic cubic B-spline prefilter runs on the GPU. ``store`` selects
+    FP64 and/or FP32 coefficient storage.
+    """
+
+    kind = QEW_FIELD_BSPLINE
+
+    def __init__(self, field, Lx: float, Ly: float, store: int = QEW_STORE_FP64,
+                 ctx: Context | None = None):
+        super().__init__()
+        self.ctx = ctx or default_context()
+        torch = _torch()
+        h = C.c_void_p()
+        if isinstance(field, torch.Tensor):
+            f = field.contiguous()
+            nx, ny = f.shape
+            _capi.check(self.ctx.lib.qew_field_create_from_device(
+                self.ctx.h, _ptr(f), nx, ny, float(Lx), float(Ly), store, C.byref(h)),
+                self.ctx.h, "FilteredNoise")
+        else:
+            f = np.ascontiguousarray(field, dtype=np.float64)
+            nx, ny = f.shape
+            _capi.check(self.ctx.lib.qew_field_create_from_host(
+                self.ctx.h, f.ctypes.data_as(_capi.PD), nx, ny, float(Lx), float(Ly), store,
+                C.byref(h)), self.ctx.h, "FilteredNoise")
+        self.h = h
+        self.nx, self.ny, self.Lx, self.Ly = nx, ny, float(Lx), float(Ly)
+        self.dx, self.dy = self.Lx / nx, self.Ly / ny
+        self.store = store
+
+    def coefficients(self) -> np.ndarray:
+        """The FP64 B-spline coefficients in the host layout [nx][ny]."""
+        out = np.empty((self.nx, self.ny))
+        _capi.check(self.ctx.lib.qew_field_get_coefficients(
+            self.ctx.h, self.h, out.ctypes.data_as(_capi.PD)), self.ctx.h, "coefficients")
+        return out
+
+    def sample(self, x, y):
+        return sample(self, x, y)
+
+
+class _Analytic(_Noise):
+    def __init__(self, kind, p0=0.0, p1=0.0, p2=0.0, ctx: Context | None = None):
+        super().__init__()
+        self.ctx = ctx or default_context()
+        self.kind = kind
+        self.params = (p0, p1, p2)
+        h = C.c_void_p()
+        _capi.check(self.ctx.lib.qew_field_create_analytic(self.ctx.h, kind, p0, p1, p2,
+                                                           C.byref(h)), self.ctx.h, "noise")
+        self.h = h
+
+    def sample(self, x, y):
+        return sample(self, x, y)
+
+
+def ZeroNoise(ctx=None):  # test_lbfgs.cpp:24-27
+    return _Analytic(QEW_FIELD_ZERO, ctx=ctx)
+
+
+def ConstNoise(v0: float = 0.0, ctx=None):  # test_qew_model.cpp:38-42
+    return _Analytic(QEW_FIELD_CONST, v0, ctx=ctx)
+
+
+def HarmonicWell(k: float = 2.0, y0: float = 0.5, ctx=None):  # test_lbfgs.cpp:30-38
+    return _Analytic(QEW_FIELD_HARMONIC, k, y0, ctx=ctx)
+
+
+def SinusoidNoise(A: float = 0.1, k: float = 2.0 * 3.14159265358979323846, ctx=None):
+    return _Analytic(QEW_FIELD_WASHBOARD, A, k, ctx=ctx)  # test_rosso_krauth.cpp:24-31
+
+
+def AnalyticNoise(amp: float = 0.3, kx: float = 0.7, ky: float = 1.3, ctx=None):
+    return _Analytic(QEW_FIELD_SINCOS, amp, kx, ky, ctx=ctx)  # test_qew_model.cpp:22-34
+
+
+def sample(noise: _Noise, x, y):
+    """DeviceNoise::sample at points (x, y): returns (v, dv_dx, dv_dy) tensors."""
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    x = torch.as_tensor(x, dtype=torch.float64, device="cuda").contiguous()
+    y = torch.as_tensor(y, dtype=torch.float64, device="cuda").contiguous()
+    v, dx, dy = torch.empty_like(x), torch.empty_like(x), torch.empty_like(x)
+    _capi.check(ctx.lib.qew_field_sample(ctx.h, noise.h, _ptr(x), _ptr(y), x.numel(), _ptr(v),
+                                         _ptr(dx), _ptr(dy)), ctx.h, "sample")
+    return v, dx, dy
+
+
+# ------------------------------------------------------------------ model
+def objective(h, p: Params, noise: _Noise) -> float:
+    ctx = noise.ctx
+    ctx.sync_stream()
+    out = C.c_double()
+    pc = p.c()
+    _capi.check(ctx.lib.qew_objective(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                      C.byref(out)), ctx.h, "objective")
+    return out.value
+
+
+def objective_trial(x0, d, alpha: float, p: Params, noise: _Noise) -> float:
+    ctx = noise.ctx
+    ctx.sync_stream()
+    out = C.c_double()
+    pc = p.c()
+    _capi.check(ctx.lib.qew_objective_trial(ctx.h, noise.h, _ptr(x0), _ptr(d), float(alpha),
+                                            x0.numel(), C.byref(pc), C.byref(out)),
+                ctx.h, "objective_trial")
+    return out.value
+
+
+def gradient(h, p: Params, noise: _Noise, grad=None, precision: int = QEW_PREC_FP64):
+    """gradient(h, p, noise, grad) -- writes and returns grad (allocated if None)."""
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    if grad is None:
+        grad = torch.empty_like(h)
+    pc = p.c()
+    _capi.check(ctx.lib.qew_gradient_prec(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                          precision, _ptr(grad)), ctx.h, "gradient")
+    return grad
+
+
+def gradient_host(h: np.ndarray, p: Params, noise: _Noise, out: np.ndarray | None = None,
+                  precision: int = QEW_PREC_FP64) -> np.ndarray:
+    """Gradient of a host (numpy, ideally pinned) line into a host array."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    if out is None:
+        out = np.empty_like(h)
+    pc = p.c()
+    _capi.check(ctx.lib.qew_gradient_host(ctx.h, noise.h, C.c_void_p(h.ctypes.data), h.size,
+                                          C.byref(pc), precision, C.c_void_p(out.ctypes.data)),
+                ctx.h, "gradient_host")
+    return out
+
+
+# ----------------------------------------------------------------- L-BFGS
+def lbfgs_minimize(h, p: Params, noise: _Noise, lp: LbfgsParams | None = None,
+                   form: int = QEW_LBFGS_RESIDENT) -> LbfgsResult:
+    """lbfgs_minimize(h, p, noise, lp): relaxes h in place (lbfgs.h:94-96)."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    lp = lp or LbfgsParams()
+    lpc, pc, res = lp.c(), p.c(), _capi.qew_lbfgs_result()
+    _capi.check(ctx.lib.qew_lbfgs_minimize_form(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                                C.byref(lpc), form, C.byref(res)),
+                ctx.h, "lbfgs_minimize")
+    return LbfgsResult(res.iterations, res.max_force, bool(res.converged), res.n_func_evals,
+                       res.n_curvature_skips, res.n_ls_restarts)
+
+
+def precond_apply(q, line_tension: float, physical_size: float, shift: float,
+                  form: int = QEW_LBFGS_RESIDENT, ctx: Context | None = None):
+    """The L-BFGS preconditioner d = M^{-1} q alone (lbfgs.h:116-146, 173-180)."""
+    torch = _torch()
+    ctx = ctx or default_context()
+    ctx.sync_stream()
+    out = torch.empty_like(q)
+    _capi.check(ctx.lib.qew_precond_apply(ctx.h, _ptr(q), q.numel(), float(line_tension),
+                                          float(physical_size), float(shift), form, _ptr(out)),
+                ctx.h, "precond_apply")
+    return out
+
+
+# --------------------------------------------------------------- Langevin
+class LangevinDynamics:
+    """LangevinDynamics(n, seed) (dynamics.h:27-70)."""
+
+    def __init__(self, n: int, seed: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        _capi.check(self.ctx.lib.qew_langevin_create(self.ctx.h, int(n), int(seed), C.byref(h)),
+                    self.ctx.h, "LangevinDynamics")
+        self.h = h
+        self.n = int(n)
+
+    def step(self, h, p: Params, noise: _Noise, drift_coeff: float, diff_coeff: float):
+        self.ctx.sync_stream()
+        if h.numel() != self.n:
+            raise ValueError("line length %d != %d" % (h.numel(), self.n))
+        pc = p.c()
+        _capi.check(self.ctx.lib.qew_langevin_step(self.h, noise.h, _ptr(h), C.byref(pc),
+                                                   float(drift_coeff), float(diff_coeff)),
+                    self.ctx.h, "langevin step")
+
+    def step_with_increments(self, h, p: Params, noise: _Noise, drift_coeff: float,
+                             diff_coeff: float, xi):
+        self.ctx.sync_stream()
+        if h.numel() != self.n or xi.numel() != self.n:
+            raise ValueError("line/increment length mismatch")
+        pc = p.c()
+        _capi.check(self.ctx.lib.qew_langevin_step_increments(
+            self.h, noise.h, _ptr(h), C.byref(pc), float(drift_coeff), float(diff_coeff),
+            _ptr(xi)), self.ctx.h, "langevin step")
+
+    def peek_increments(self):
+        torch = _torch()
+        self.ctx.sync_stream()
+        out = torch.empty(self.n, dtype=torch.float64, device="cuda")
+        _capi.check(self.ctx.lib.qew_langevin_peek_increments(self.h, _ptr(out)), self.ctx.h,
+                    "peek_increments")
+        return out
+
+    @property
+    def steps(self) -> int:
+        return int(self.ctx.lib.qew_langevin_steps(self.h))
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.ctx.lib.qew_langevin_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------- Rosso-Krauth
+def rk_site_velocity(h, p: Params, noise: _Noise):
+    """rk_site_velocity (rosso_krauth.h:51-82) of every site of h."""
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    out = torch.empty_like(h)
+    pc = p.c()
+    _capi.check(ctx.lib.qew_rk_site_velocity(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                             _ptr(out)), ctx.h, "rk_site_velocity")
+    return out
+
+
+def rk_block(h, p: Params, noise: _Noise, rp: RkParams) -> RkResult:
+    """rk_block(h, p, noise, rp) (rosso_krauth.h:128-194); ValueError on odd n."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    pc, rpc, res = p.c(), rp.c(), _capi.qew_rk_result()
+    _capi.check(ctx.lib.qew_rk_block(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                     C.byref(rpc), C.byref(res)), ctx.h, "rk_block")
+    return RkResult(bool(res.blocked), bool(res.runaway), res.sweeps, res.total_advance,
+                    res.mean_h)
+
+
+def depinning_bisect(h, p: Params, noise: _Noise, rp: RkParams, f_lo: float, f_hi: float,
+                     rtol: float = 1e-10, max_steps: int = 200):
+    """Bisect the depinning force from a blocked h at f_lo; see qew_gpu.h."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    pc, rpc = p.c(), rp.c()
+    fc, flo, fhi, nb = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+    _capi.check(ctx.lib.qew_depinning_bisect(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                             C.byref(rpc), float(f_lo), float(f_hi), float(rtol),
+                                             int(max_steps), C.byref(fc), C.byref(flo),
+                                             C.byref(fhi), C.byref(nb)), ctx.h,
+                "depinning_bisect")
+    return fc.value, flo.value, fhi.value, nb.value

@@ -1,0 +1,146 @@
+"""ctypes binding of the C ABI in ``include/qew_gpu.h``.
+
+Loads the in-tree ``_lib/libqew_gb300.so``. There is no fallback: if the
+library is missing or cannot be loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libqew_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "qew_gpu.h")
+
+D, I, U64, VP = C.c_double, C.c_int, C.c_uint64, C.c_void_p
+PD = C.POINTER(C.c_double)
+
+QEW_OK = 0
+QEW_ERR_INVALID = 1
+QEW_ERR_ODD_LENGTH = 2
+QEW_ERR_CUDA = 3
+QEW_ERR_NOMEM = 4
+QEW_ERR_TIMEOUT = 5
+QEW_ERR_UNSUPPORTED = 6
+
+QEW_FIELD_BSPLINE, QEW_FIELD_ZERO, QEW_FIELD_CONST = 0, 1, 2
+QEW_FIELD_HARMONIC, QEW_FIELD_WASHBOARD, QEW_FIELD_SINCOS = 3, 4, 5
+QEW_STORE_FP64, QEW_STORE_FP32 = 1, 2
+QEW_PREC_FP64, QEW_PREC_FP32_SPLIT = 0, 1
+QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
+
+
+class qew_params(C.Structure):
+    _fields_ = [("physical_size", D), ("line_tension", D), ("driving_force", D), ("model", I)]
+
+
+class qew_lbfgs_params(C.Structure):
+    _fields_ = [("m", I), ("ftol", D), ("max_iter", I), ("c1", D), ("ls_shrink", D),
+                ("max_ls", I), ("curvature_eps", D), ("precondition", I), ("precond_shift", D)]
+
+
+class qew_lbfgs_result(C.Structure):
+    _fields_ = [("iterations", I), ("max_force", D), ("converged", I),
+                ("n_func_evals", C.c_long), ("n_curvature_skips", C.c_long),
+                ("n_ls_restarts", C.c_long)]
+
+
+class qew_rk_params(C.Structure):
+    _fields_ = [("dstep", D), ("max_advance", D), ("root_tol", D), ("sweep_tol", D),
+                ("runaway", D), ("max_sweeps", I)]
+
+
+class qew_rk_result(C.Structure):
+    _fields_ = [("blocked", I), ("runaway", I), ("sweeps", I), ("total_advance", D),
+                ("mean_h", D)]
+
+
+class QewError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+_lib = None
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "qew_status_string": (C.c_char_p, [I]),
+    "qew_ctx_create": (I, [I, C.POINTER(VP)]),
+    "qew_ctx_destroy": (I, [VP]),
+    "qew_ctx_set_stream": (I, [VP, VP]),
+    "qew_ctx_synchronize": (I, [VP]),
+    "qew_last_error": (C.c_char_p, [VP]),
+    "qew_ctx_launch_count": (U64, [VP]),
+    "qew_field_create_from_host": (I, [VP, PD, I, I, D, D, I, C.POINTER(VP)]),
+    "qew_field_create_from_device": (I, [VP, VP, I, I, D, D, I, C.POINTER(VP)]),
+    "qew_field_create_analytic": (I, [VP, I, D, D, D, C.POINTER(VP)]),
+    "qew_field_destroy": (I, [VP]),
+    "qew_field_get_coefficients": (I, [VP, VP, PD]),
+    "qew_field_sample": (I, [VP, VP, VP, VP, I, VP, VP, VP]),
+    "qew_objective": (I, [VP, VP, VP, I, C.POINTER(qew_params), PD]),
+    "qew_objective_trial": (I, [VP, VP, VP, VP, D, I, C.POINTER(qew_params), PD]),
+    "qew_gradient": (I, [VP, VP, VP, I, C.POINTER(qew_params), VP]),
+    "qew_gradient_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
+    "qew_gradient_host": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
+    "qew_lbfgs_default_params": (I, [C.POINTER(qew_lbfgs_params)]),
+    "qew_lbfgs_minimize": (I, [VP, VP, VP, I, C.POINTER(qew_params),
+                               C.POINTER(qew_lbfgs_params), C.POINTER(qew_lbfgs_result)]),
+    "qew_lbfgs_minimize_form": (I, [VP, VP, VP, I, C.POINTER(qew_params),
+                                    C.POINTER(qew_lbfgs_params), I,
+                                    C.POINTER(qew_lbfgs_result)]),
+    "qew_precond_apply": (I, [VP, VP, I, D, D, D, I, VP]),
+    "qew_langevin_create": (I, [VP, I, U64, C.POINTER(VP)]),
+    "qew_langevin_destroy": (I, [VP]),
+    "qew_langevin_step": (I, [VP, VP, VP, C.POINTER(qew_params), D, D]),
+    "qew_langevin_step_increments": (I, [VP, VP, VP, C.POINTER(qew_params), D, D, VP]),
+    "qew_langevin_peek_increments": (I, [VP, VP]),
+    "qew_langevin_steps": (U64, [VP]),
+    "qew_rk_site_velocity": (I, [VP, VP, VP, I, C.POINTER(qew_params), VP]),
+    "qew_rk_block": (I, [VP, VP, VP, I, C.POINTER(qew_params), C.POINTER(qew_rk_params),
+                         C.POINTER(qew_rk_result)]),
+    "qew_depinning_bisect": (I, [VP, VP, VP, I, C.POINTER(qew_params),
+                                 C.POINTER(qew_rk_params), D, D, D, I, PD, PD, PD,
+                                 C.POINTER(I)]),
+}
+
+
+def header_symbols() -> list[str]:
+    """Every function the public header declares."""
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(qew_[a-z0-9_]+)\s*\(",
+                                 txt, re.M)))
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library (raises if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("qew_gb300: CUDA library %s is not built; run "
+                           "qew_gb300.build.build() (there is no CPU fallback)" % path)
+    lib = C.CDLL(path)
+    for name, (rt, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = rt
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int, ctx=None, what: str = "") -> None:
+    if status == QEW_OK:
+        return
+    lib = load()
+    msg = lib.qew_status_string(status).decode()
+    if ctx is not None:
+        detail = lib.qew_last_error(ctx).decode()
+        if detail:
+            msg = detail
+    if what:
+        msg = what + ": " + msg
+    if status in (QEW_ERR_INVALID, QEW_ERR_ODD_LENGTH):
+        raise ValueError(msg)
+    raise QewError(status, msg)

@@ -1,0 +1,85 @@
+"""Build the GB300 qEW CUDA library in-tree.
+
+Compiles every ``csrc/*.cu`` for sm_103a with nvcc (in parallel, one object
+per translation unit) and links ``_lib/libqew_gb300.so``, which exports the C
+ABI declared in ``include/qew_gpu.h``. cudart is linked statically; cuFFT
+(used only by the host-driven comparator form of L-BFGS) dynamically, with an
+rpath to the toolkit's library directory.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import glob
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "_lib")
+OBJ_DIR = os.path.join(OUT_DIR, "obj")
+LIB = os.path.join(OUT_DIR, "libqew_gb300.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unknown-pragmas"]
+
+
+def _cuda_home() -> str:
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "bin", "nvcc")):
+            return c
+    nvcc = shutil.which("nvcc")
+    if nvcc:
+        return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    raise RuntimeError("nvcc not found")
+
+
+def _headers():
+    return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+
+
+def _stale(lib: str, srcs) -> bool:
+    if not os.path.exists(lib):
+        return True
+    t = os.path.getmtime(lib)
+    return any(os.path.getmtime(s) > t for s in list(srcs) + _headers() + [__file__])
+
+
+def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
+    srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    if not force and not _stale(LIB, srcs):
+        return LIB
+    cuda = _cuda_home()
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    flags = ARCH + NVCC_FLAGS + ["-I" + INCLUDE] + list(extra_flags or [])
+
+    def compile_one(src):
+        obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+        cmd = [nvcc] + flags + ["-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
+        if verbose and r.stderr.strip():
+            print(r.stderr, file=sys.stderr)
+        return obj
+
+    workers = min(len(srcs), max(1, os.cpu_count() or 1))
+    with cf.ThreadPoolExecutor(workers) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    libdir = os.path.join(cuda, "lib64")
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + [
+        "-L" + libdir, "-lcufft", "-Xlinker", "-rpath," + libdir]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,326 @@
+// qew_internal.cuh -- shared internals of the GB300 qEW library: context and
+// field handles, error plumbing, and the device-side Noise functors.
+//
+// Noise functors mirror the reference's `Noise` concept (qew_model.h:14-17,
+// 31-48): a copyable, device-callable object with value / dV/dy / full
+// sample. NoiseBSpline64 restates DeviceNoise (filtered_noise.h:67-177) on an
+// x-fastest coefficient array, keeping the reference's exact coordinate
+// arithmetic (x/dx, periodic fold, floor) so the cell index and fraction are
+// bit-identical to the reference's; only the weight polynomials use
+// multiplications by 1/6 where the reference divides (a <= 1 ulp change).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "../../include/qew_gpu.h"
+
+// ---------------------------------------------------------------- handles
+struct qew_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    // reduction scratch: per-block partials + a self-resetting ticket counter
+    double *red_partials = nullptr;  // QEW_RED_MAX_BLOCKS * 4 doubles
+    unsigned int *red_counter = nullptr;
+    double *red_out = nullptr;       // 8 doubles of device results
+    double *host_out = nullptr;      // pinned 8 doubles
+    // general scratch arena (grown on demand, never shrunk)
+    void *scratch = nullptr;
+    size_t scratch_bytes = 0;
+    uint64_t launches = 0;
+    std::string last_error;
+};
+
+struct qew_field {
+    int kind = QEW_FIELD_BSPLINE;
+    int device = 0;
+    int nx = 0, ny = 0;
+    double Lx = 0, Ly = 0, dx = 1, dy = 1;
+    double p0 = 0, p1 = 0, p2 = 0;
+    double *coef64 = nullptr;  // [ny][nx], x fastest
+    float *coef32 = nullptr;   // [ny][nx], x fastest
+};
+
+#define QEW_RED_MAX_BLOCKS 1024
+
+// Records the message on ctx (if any) and returns the status.
+qew_status qew_fail(qew_ctx *ctx, qew_status s, const char *fmt, ...);
+// Ensures ctx->scratch holds at least `bytes` (256-byte aligned base).
+qew_status qew_scratch_reserve(qew_ctx *ctx, size_t bytes);
+// Checks the last launch; bumps the launch counter by `k`.
+qew_status qew_launch_check(qew_ctx *ctx, const char *what, int k = 1);
+
+#define QEW_CUDA(ctx, call)                                                  \
+    do {                                                                     \
+        cudaError_t e__ = (call);                                            \
+        if (e__ != cudaSuccess)                                              \
+            return qew_fail((ctx), QEW_ERR_CUDA, "%s: %s", #call,            \
+                            cudaGetErrorString(e__));                        \
+    } while (0)
+
+#define QEW_TRY(expr)                                                        \
+    do {                                                                     \
+        qew_status s__ = (expr);                                             \
+        if (s__ != QEW_OK) return s__;                                       \
+    } while (0)
+
+// ------------------------------------------------------------ B-spline math
+// Cubic B-spline weights for neighbours {i-1,i,i+1,i+2} at fraction t
+// (filtered_noise.h:33-46), and their t-derivatives (filtered_noise.h:50-62).
+__device__ __forceinline__ void bsw_value(double t, double w[4]) {
+    const double s6 = 1.0 / 6.0;
+    const double t2 = t * t, t3 = t2 * t, omt = 1.0 - t;
+    w[0] = omt * omt * omt * s6;
+    w[1] = (4.0 - 6.0 * t2 + 3.0 * t3) * s6;
+    w[2] = (1.0 + 3.0 * t + 3.0 * t2 - 3.0 * t3) * s6;
+    w[3] = t3 * s6;
+}
+__device__ __forceinline__ void bsw_deriv(double t, double dw[4]) {
+    const double s6 = 1.0 / 6.0;
+    const double t2 = t * t, omt = 1.0 - t;
+    dw[0] = -omt * omt * 0.5;
+    dw[1] = (-12.0 * t + 9.0 * t2) * s6;
+    dw[2] = (3.0 + 6.0 * t - 9.0 * t2) * s6;
+    dw[3] = 3.0 * t2 * s6;
+}
+
+// Physical -> grid coordinate along one axis with the periodic fold of
+// DeviceNoise::locate (filtered_noise.h:80-92). Division by the spacing is
+// replaced by a multiplication only when the spacing is a power of two
+// (then both are exact); the fold is skipped when g is already in [0, n)
+// (then floor(g/n) == 0 exactly, so the result is the same).
+__device__ __forceinline__ void grid_locate(double x, double d, double inv_d,
+                                            bool d_pow2, int n, int &ix,
+                                            double &fx) {
+    double g = d_pow2 ? x * inv_d : x / d;
+    const double nd = (double)n;
+    if (!(g >= 0.0 && g < nd)) g -= floor(g / nd) * nd;
+    ix = (int)floor(g);
+    if (ix >= n) {
+        ix -= n;
+        g -= nd;
+    }
+    fx = g - (double)ix;
+    // Only a non-finite coordinate can leave [0, n) here; clamp so the
+    // gather stays in bounds whatever the input (a no-op for finite x).
+    ix = min(max(ix, 0), n - 1);
+}
+
+__device__ __forceinline__ void wrap4(int i, int n, int o[4]) {
+    o[0] = (i == 0) ? n - 1 : i - 1;
+    o[1] = i;
+    o[2] = (i + 1 == n) ? 0 : i + 1;
+    o[3] = (o[2] + 1 == n) ? 0 : o[2] + 1;
+}
+
+// DeviceNoise on x-fastest FP64 coefficients.
+struct NoiseBSpline64 {
+    const double *__restrict__ coef;  // [ny][nx]
+    int nx, ny;
+    double dx, dy, inv_dx, inv_dy;
+    bool dx_pow2, dy_pow2;
+
+    __device__ __forceinline__ double c(int ix, int iy) const {
+        return __ldg(coef + (size_t)iy * (size_t)nx + ix);
+    }
+    __device__ __forceinline__ void locate(double x, double y, int ixn[4],
+                                           int iyn[4], double &fx,
+                                           double &fy) const {
+        int ix, iy;
+        grid_locate(x, dx, inv_dx, dx_pow2, nx, ix, fx);
+        grid_locate(y, dy, inv_dy, dy_pow2, ny, iy, fy);
+        wrap4(ix, nx, ixn);
+        wrap4(iy, ny, iyn);
+    }
+    // sample_value, filtered_noise.h:138-155
+    __device__ __forceinline__ double value(double x, double y) const {
+        int ixn[4], iyn[4];
+        double fx, fy, wx[4], wy[4];
+        locate(x, y, ixn, iyn, fx, fy);
+        bsw_value(fx, wx);
+        bsw_value(fy, wy);
+        double v = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) row += c(ixn[a], iyn[b]) * wy[b];
+            v += wx[a] * row;
+        }
+        return v;
+    }
+    // sample_dy, filtered_noise.h:159-176
+    __device__ __forceinline__ double dvdy(double x, double y) const {
+        int ixn[4], iyn[4];
+        double fx, fy, wx[4], dwy[4];
+        locate(x, y, ixn, iyn, fx, fy);
+        bsw_value(fx, wx);
+        bsw_deriv(fy, dwy);
+        double dg = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) row += c(ixn[a], iyn[b]) * dwy[b];
+            dg += wx[a] * row;
+        }
+        return dy_pow2 ? dg * inv_dy : dg / dy;
+    }
+    // sample, filtered_noise.h:103-134
+    __device__ __forceinline__ void sample(double x, double y, double &v,
+                                           double &dvdx_,
+                                           double &dvdy_) const {
+        int ixn[4], iyn[4];
+        double fx, fy, wx[4], dwx[4], wy[4], dwy[4];
+        locate(x, y, ixn, iyn, fx, fy);
+        bsw_value(fx, wx);
+        bsw_deriv(fx, dwx);
+        bsw_value(fy, wy);
+        bsw_deriv(fy, dwy);
+        double vv = 0, gx = 0, gy = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0, row_dy = 0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const double cc = c(ixn[a], iyn[b]);
+                row += cc * wy[b];
+                row_dy += cc * dwy[b];
+            }
+            vv += wx[a] * row;
+            gx += dwx[a] * row;
+            gy += wx[a] * row_dy;
+        }
+        v = vv;
+        dvdx_ = dx_pow2 ? gx * inv_dx : gx / dx;
+        dvdy_ = dy_pow2 ? gy * inv_dy : gy / dy;
+    }
+};
+
+// Analytic potentials of the reference's tests; value()/dvdy() go through
+// sample() exactly like detail::noise_value/noise_dvdy (qew_model.h:31-46).
+struct NoiseZero {
+    __device__ __forceinline__ void sample(double, double, double &v,
+                                           double &a, double &b) const {
+        v = 0; a = 0; b = 0;
+    }
+    __device__ __forceinline__ double value(double, double) const { return 0; }
+    __device__ __forceinline__ double dvdy(double, double) const { return 0; }
+};
+struct NoiseConst {
+    double v0;
+    __device__ __forceinline__ void sample(double, double, double &v,
+                                           double &a, double &b) const {
+        v = v0; a = 0; b = 0;
+    }
+    __device__ __forceinline__ double value(double, double) const { return v0; }
+    __device__ __forceinline__ double dvdy(double, double) const { return 0; }
+};
+struct NoiseHarmonic {  // HarmonicWell{k, y0}
+    double k, y0;
+    __device__ __forceinline__ void sample(double, double y, double &v,
+                                           double &a, double &b) const {
+        const double d = y - y0;
+        v = 0.5 * k * d * d; a = 0; b = k * d;
+    }
+    __device__ __forceinline__ double value(double, double y) const {
+        const double d = y - y0;
+        return 0.5 * k * d * d;
+    }
+    __device__ __forceinline__ double dvdy(double, double y) const {
+        return k * (y - y0);
+    }
+};
+struct NoiseWashboard {  // SinusoidNoise{A, k}: V = A cos(k y)
+    double A, k;
+    __device__ __forceinline__ void sample(double, double y, double &v,
+                                           double &a, double &b) const {
+        v = A * cos(k * y); a = 0; b = -A * k * sin(k * y);
+    }
+    __device__ __forceinline__ double value(double, double y) const {
+        return A * cos(k * y);
+    }
+    __device__ __forceinline__ double dvdy(double, double y) const {
+        return -A * k * sin(k * y);
+    }
+};
+struct NoiseSinCos {  // AnalyticNoise{amp, kx, ky}
+    double amp, kx, ky;
+    __device__ __forceinline__ void sample(double x, double y, double &v,
+                                           double &a, double &b) const {
+        v = amp * sin(kx * x) * cos(ky * y);
+        a = amp * kx * cos(kx * x) * cos(ky * y);
+        b = -amp * ky * sin(kx * x) * sin(ky * y);
+    }
+    __device__ __forceinline__ double value(double x, double y) const {
+        return amp * sin(kx * x) * cos(ky * y);
+    }
+    __device__ __forceinline__ double dvdy(double x, double y) const {
+        return -amp * ky * sin(kx * x) * sin(ky * y);
+    }
+};
+
+// Host helpers building the functors from a field handle.
+static inline bool qew_is_pow2(double d) {
+    int e;
+    const double m = frexp(d, &e);
+    return d > 0 && m == 0.5;
+}
+static inline NoiseBSpline64 make_bspline64(const qew_field *f) {
+    NoiseBSpline64 nz;
+    nz.coef = f->coef64;
+    nz.nx = f->nx;
+    nz.ny = f->ny;
+    nz.dx = f->dx;
+    nz.dy = f->dy;
+    nz.inv_dx = 1.0 / f->dx;
+    nz.inv_dy = 1.0 / f->dy;
+    nz.dx_pow2 = qew_is_pow2(f->dx);
+    nz.dy_pow2 = qew_is_pow2(f->dy);
+    return nz;
+}
+
+// Calls `fn(noise_functor)` with the functor matching the field's kind.
+// Returns QEW_ERR_INVALID for an unknown kind or a B-spline field without
+// FP64 coefficients.
+template <class Fn>
+qew_status qew_dispatch_noise(qew_ctx *ctx, const qew_field *f, Fn &&fn) {
+    switch (f->kind) {
+    case QEW_FIELD_BSPLINE:
+        if (!f->coef64)
+            return qew_fail(ctx, QEW_ERR_INVALID,
+                            "field has no FP64 coefficients (created without "
+                            "QEW_STORE_FP64)");
+        return fn(make_bspline64(f));
+    case QEW_FIELD_ZERO: return fn(NoiseZero{});
+    case QEW_FIELD_CONST: return fn(NoiseConst{f->p0});
+    case QEW_FIELD_HARMONIC: return fn(NoiseHarmonic{f->p0, f->p1});
+    case QEW_FIELD_WASHBOARD: return fn(NoiseWashboard{f->p0, f->p1});
+    case QEW_FIELD_SINCOS: return fn(NoiseSinCos{f->p0, f->p1, f->p2});
+    default:
+        return qew_fail(ctx, QEW_ERR_INVALID, "unknown field kind %d", f->kind);
+    }
+}
+
+// ------------------------------------------------------ block reductions
+template <int BS>
+__device__ __forceinline__ double block_sum(double v, double *s_warp) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) s_warp[w] = v;
+    __syncthreads();
+    double r = 0;
+    if (w == 0) {
+        r = (lane < BS / 32) ? s_warp[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    }
+    __syncthreads();
+    return r;  // valid in thread 0
+}

@@ -1,0 +1,247 @@
+// qew_lbfgs_resident.cuh -- one CTA runs one complete lbfgs_minimize
+// (lbfgs.h:94-287). Shared by the single-line entry point and the batched
+// ensemble kernel.
+#pragma once
+
+#include "qew_block.cuh"
+
+constexpr int kLbfgsMaxM = 32;
+constexpr int kLbfgsVecs = 6;  // g, g_new, d, q, edge dV/dy, edge slope
+
+struct LbfgsCfg {
+    int m;
+    double ftol;
+    int max_iter;
+    double c1;
+    double ls_shrink;
+    int max_ls;
+    double curvature_eps;
+    int precondition;
+};
+
+inline LbfgsCfg lbfgs_cfg_from(const qew_lbfgs_params *lp) {
+    LbfgsCfg c;
+    c.m = lp->m;
+    c.ftol = lp->ftol;
+    c.max_iter = lp->max_iter;
+    c.c1 = lp->c1;
+    c.ls_shrink = lp->ls_shrink;
+    c.max_ls = lp->max_ls;
+    c.curvature_eps = lp->curvature_eps;
+    c.precondition = lp->precondition;
+    return c;
+}
+
+inline size_t lbfgs_block_smem_bytes(int /*bs*/, int /*m*/) { return 0; }
+
+// History bookkeeping of lbfgs.h:107-114, 262-279: `slots` in chronological
+// order, and buffer indices standing in for the reference's View swaps.
+struct LbfgsShared {
+    double rho[kLbfgsMaxM];
+    double la[kLbfgsMaxM];
+    int slots[kLbfgsMaxM];
+    int sbuf[kLbfgsMaxM];
+    int ybuf[kLbfgsMaxM];
+    int nslots;
+    int stmp;
+    int ytmp;
+};
+
+// Workspace (npad-strided vectors): g, g_new, d, q, ev, es, then 2(m+1)
+// history buffers (m S rows + spare, m Y rows + spare).
+template <class Noise, int BS>
+__device__ void lbfgs_block(const Noise &nz, double *__restrict__ h, const int n,
+                            const qew_params P, const LbfgsCfg cfg, const PrecondCoef pc,
+                            double *ws, size_t npad, qew_lbfgs_result *out, double * /*dyn*/) {
+    __shared__ double s_w[96];
+    __shared__ double s_b[BS];
+    __shared__ LbfgsShared sh;
+    const int t = threadIdx.x;
+    const double dx = P.physical_size / (double)n;
+    const double lt = P.line_tension, f = P.driving_force;
+    const int model = P.model;
+    const bool arc = (model == QEW_MODEL_ARCLENGTH);
+    double *g = ws, *gn = ws + npad, *d = ws + 2 * npad, *q = ws + 3 * npad;
+    double *ev = ws + 4 * npad, *es = ws + 5 * npad;
+    double *bufs = ws + (size_t)kLbfgsVecs * npad;
+    const int m = cfg.m;
+    if (t == 0) {
+        sh.nslots = 0;
+        for (int k = 0; k < m; ++k) {
+            sh.sbuf[k] = k;
+            sh.ybuf[k] = m + 1 + k;
+        }
+        sh.stmp = m;
+        sh.ytmp = 2 * m + 1;
+    }
+    __syncthreads();
+
+    qew_lbfgs_result res;
+    res.iterations = 0;
+    res.max_force = 0;
+    res.converged = 0;
+    res.n_func_evals = 0;
+    res.n_curvature_skips = 0;
+    res.n_ls_restarts = 0;
+    double gamma = 1.0;
+    int ls_fail_streak = 0;
+    double phi = 0.0;
+    bool done = false;
+
+    block_gradient<Noise, BS>(nz, h, n, dx, lt, f, arc, ev, es, g);
+
+    for (int it = 0; it < cfg.max_iter; ++it) {
+        double lm = 0.0;
+        for (int i = t; i < n; i += BS) lm = fmax(lm, fabs(g[i]));
+        const double gmax = bmax_all<BS>(lm, s_w);
+        if (gmax < cfg.ftol) {  // lbfgs.h:155-161
+            res.iterations = it;
+            res.max_force = gmax;
+            res.converged = 1;
+            done = true;
+            break;
+        }
+        // two-loop recursion, lbfgs.h:163-191
+        for (int i = t; i < n; i += BS) q[i] = g[i];
+        __syncthreads();
+        const int hs = sh.nslots;
+        for (int idx = hs - 1; idx >= 0; --idx) {
+            const int row = sh.slots[idx];
+            const double *S = bufs + (size_t)sh.sbuf[row] * npad;
+            const double *Y = bufs + (size_t)sh.ybuf[row] * npad;
+            double acc = 0.0;
+            for (int i = t; i < n; i += BS) acc += S[i] * q[i];
+            const double a = sh.rho[row] * bsum_all<BS>(acc, s_w);
+            if (t == 0) sh.la[idx] = a;
+            for (int i = t; i < n; i += BS) q[i] += -a * Y[i];
+            __syncthreads();
+        }
+        if (cfg.precondition) {
+            block_precond<BS>(q, d, n, pc, s_b, s_w);
+        } else {
+            const double g0 = (hs == 0) ? 1.0 : gamma;
+            for (int i = t; i < n; i += BS) d[i] = g0 * q[i];
+            __syncthreads();
+        }
+        for (int idx = 0; idx < hs; ++idx) {
+            const int row = sh.slots[idx];
+            const double *S = bufs + (size_t)sh.sbuf[row] * npad;
+            const double *Y = bufs + (size_t)sh.ybuf[row] * npad;
+            double acc = 0.0;
+            for (int i = t; i < n; i += BS) acc += Y[i] * d[i];
+            const double b = sh.rho[row] * bsum_all<BS>(acc, s_w);
+            const double c = sh.la[idx] - b;
+            for (int i = t; i < n; i += BS) d[i] += c * S[i];
+            __syncthreads();
+        }
+        // d = -d, fused with dphi0 = g.d (lbfgs.h:190-194)
+        double acc = 0.0;
+        for (int i = t; i < n; i += BS) {
+            const double v = -d[i];
+            d[i] = v;
+            acc += g[i] * v;
+        }
+        double dphi0 = bsum_all<BS>(acc, s_w);
+        bool empty = (hs == 0);
+        if (dphi0 >= 0) {  // steepest-descent fallback, lbfgs.h:195-200
+            if (t == 0) sh.nslots = 0;
+            empty = true;
+            double gg = 0.0;
+            for (int i = t; i < n; i += BS) {
+                d[i] = -g[i];
+                gg += g[i] * g[i];
+            }
+            dphi0 = -bsum_all<BS>(gg, s_w);
+        }
+        // Armijo backtracking, lbfgs.h:202-238
+        if (it == 0) {
+            phi = block_objective<Noise, BS>(nz, h, d, 0.0, n, dx, lt, f, model, s_w);
+            ++res.n_func_evals;
+        }
+        const double phi0 = phi;
+        double alpha = 1.0;
+        if (!cfg.precondition && empty) {
+            double gg = 0.0;
+            for (int i = t; i < n; i += BS) gg += g[i] * g[i];
+            alpha = 1.0 / fmax(1.0, sqrt(bsum_all<BS>(gg, s_w)));
+        }
+        bool ok = false;
+        for (int ls = 0; ls < cfg.max_ls; ++ls) {
+            const double pt = block_objective<Noise, BS>(nz, h, d, alpha, n, dx, lt, f, model, s_w);
+            ++res.n_func_evals;
+            if (pt <= phi0 + cfg.c1 * alpha * dphi0) {
+                phi = pt;
+                ok = true;
+                break;
+            }
+            alpha *= cfg.ls_shrink;
+        }
+        if (!ok) {
+            if (empty || ++ls_fail_streak > 2) {
+                res.iterations = it;
+                res.max_force = gmax;
+                res.converged = 0;
+                done = true;
+                break;
+            }
+            if (t == 0) sh.nslots = 0;
+            ++res.n_ls_restarts;
+            __syncthreads();
+            continue;
+        }
+        ls_fail_streak = 0;
+        for (int i = t; i < n; i += BS) h[i] += alpha * d[i];  // lbfgs.h:243-244
+        __syncthreads();
+        block_gradient<Noise, BS>(nz, h, n, dx, lt, f, arc, ev, es, gn);
+        double *sT = bufs + (size_t)sh.stmp * npad;
+        double *yT = bufs + (size_t)sh.ytmp * npad;
+        double sy = 0.0, ss = 0.0, yy = 0.0;
+        for (int i = t; i < n; i += BS) {  // lbfgs.h:250-261
+            const double s = alpha * d[i];
+            const double y = gn[i] - g[i];
+            sT[i] = s;
+            yT[i] = y;
+            sy += s * y;
+            ss += s * s;
+            yy += y * y;
+        }
+        bsum3_all<BS>(sy, ss, yy, s_w);
+        if (sy > cfg.curvature_eps * sqrt(ss * yy)) {  // lbfgs.h:262-279
+            if (t == 0) {
+                int row;
+                if (sh.nslots < m) {
+                    row = sh.nslots;
+                } else {
+                    row = sh.slots[0];
+                    for (int k = 0; k + 1 < sh.nslots; ++k) sh.slots[k] = sh.slots[k + 1];
+                    --sh.nslots;
+                }
+                int tmp = sh.sbuf[row];
+                sh.sbuf[row] = sh.stmp;
+                sh.stmp = tmp;
+                tmp = sh.ybuf[row];
+                sh.ybuf[row] = sh.ytmp;
+                sh.ytmp = tmp;
+                sh.rho[row] = 1.0 / sy;
+                sh.slots[sh.nslots++] = row;
+            }
+            gamma = sy / yy;
+        } else {
+            ++res.n_curvature_skips;
+        }
+        __syncthreads();
+        double *tg = g;
+        g = gn;
+        gn = tg;
+    }
+    if (!done) {  // lbfgs.h:283-286
+        double lm = 0.0;
+        for (int i = t; i < n; i += BS) lm = fmax(lm, fabs(g[i]));
+        res.iterations = cfg.max_iter;
+        res.max_force = bmax_all<BS>(lm, s_w);
+        res.converged = 0;
+    }
+    if (t == 0) *out = res;
+}
+
+size_t qew_lbfgs_resident_ws_doubles(int n, int m);

@@ -1,0 +1,108 @@
+// qew_model.cu -- energy and gradient of the periodic line (qew_model.h).
+//
+// gradient: the reference runs two kernels, an edge pass writing dV/dy (and
+// the arclength slope) of every edge to scratch and a per-site combine
+// (qew_model.h:163-193). Here one kernel does both: each CTA computes the
+// edges of its sites plus one halo edge into shared memory, then combines, so
+// the per-edge scratch never touches HBM and one launch replaces two.
+//
+// objective: the per-edge energy (qew_model.h:61-83) reduced by a fixed
+// grid-stride / warp-shuffle / CTA tree with a last-block final sum, so the
+// result is bit-reproducible for a given n regardless of scheduling.
+#include "qew_internal.cuh"
+#include "qew_model_kernels.cuh"
+
+namespace {
+
+constexpr int kGradBS = 256;
+constexpr int kObjBS = 256;
+
+int objective_blocks(int n) {
+    int b = (n + kObjBS - 1) / kObjBS;
+    return b < QEW_RED_MAX_BLOCKS ? (b > 0 ? b : 1) : QEW_RED_MAX_BLOCKS;
+}
+
+template <class At>
+qew_status objective_impl(qew_ctx *ctx, const qew_field *field, const At &at, int n,
+                          const qew_params *p, double *h_out) {
+    if (!ctx || !field || !p || !h_out || n < 1)
+        return qew_fail(ctx, QEW_ERR_INVALID, "objective: bad arguments");
+    const double dx = p->physical_size / (double)n;
+    const int blocks = objective_blocks(n);
+    QEW_TRY(qew_dispatch_noise(ctx, field, [&](auto nz) -> qew_status {
+        k_objective<decltype(nz), At, kObjBS><<<blocks, kObjBS, 0, ctx->stream>>>(
+            n, dx, p->line_tension, p->driving_force, p->model, nz, at, ctx->red_partials,
+            ctx->red_counter, ctx->red_out);
+        return qew_launch_check(ctx, "objective");
+    }));
+    QEW_CUDA(ctx, cudaMemcpyAsync(ctx->host_out, ctx->red_out, sizeof(double),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
+    QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *h_out = ctx->host_out[0];
+    return QEW_OK;
+}
+
+}  // namespace
+
+qew_status qew_gradient_enqueue(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
+                                const qew_params *p, int precision, double *d_grad) {
+    if (!ctx || !field || !p || !d_h || !d_grad || n < 1)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient: bad arguments");
+    const double dx = p->physical_size / (double)n;
+    const int blocks = (n + kGradBS - 1) / kGradBS;
+    if (precision == QEW_PREC_FP32_SPLIT) {
+        if (field->kind != QEW_FIELD_BSPLINE || !field->coef32)
+            return qew_fail(ctx, QEW_ERR_INVALID,
+                            "gradient: FP32 split gather needs a B-spline field stored with QEW_STORE_FP32");
+        return qew_gradient_split_enqueue(ctx, field, d_h, n, p, d_grad);
+    }
+    if (precision != QEW_PREC_FP64)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient: unknown precision %d", precision);
+    return qew_dispatch_noise(ctx, field, [&](auto nz) -> qew_status {
+        k_gradient<decltype(nz), kGradBS><<<blocks, kGradBS, 0, ctx->stream>>>(
+            d_h, n, dx, p->line_tension, p->driving_force, p->model, nz, d_grad);
+        return qew_launch_check(ctx, "gradient");
+    });
+}
+
+extern "C" {
+
+qew_status qew_objective(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
+                         const qew_params *p, double *h_out) {
+    if (!d_h) return qew_fail(ctx, QEW_ERR_INVALID, "objective: null h");
+    return objective_impl(ctx, field, LineAt{d_h}, n, p, h_out);
+}
+
+qew_status qew_objective_trial(qew_ctx *ctx, const qew_field *field, const double *d_x0,
+                               const double *d_d, double alpha, int n, const qew_params *p,
+                               double *h_out) {
+    if (!d_x0 || !d_d) return qew_fail(ctx, QEW_ERR_INVALID, "objective_trial: null input");
+    return objective_impl(ctx, field, TrialAt{d_x0, d_d, alpha}, n, p, h_out);
+}
+
+qew_status qew_gradient(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
+                        const qew_params *p, double *d_grad) {
+    return qew_gradient_enqueue(ctx, field, d_h, n, p, QEW_PREC_FP64, d_grad);
+}
+
+qew_status qew_gradient_prec(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
+                             const qew_params *p, int precision, double *d_grad) {
+    return qew_gradient_enqueue(ctx, field, d_h, n, p, precision, d_grad);
+}
+
+qew_status qew_gradient_host(qew_ctx *ctx, const qew_field *field, const double *h_h, int n,
+                             const qew_params *p, int precision, double *h_grad) {
+    if (!ctx || !h_h || !h_grad || n < 1)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient_host: bad arguments");
+    const size_t bytes = sizeof(double) * (size_t)n;
+    QEW_TRY(qew_scratch_reserve(ctx, 2 * bytes + 256));
+    double *d_h = (double *)ctx->scratch;
+    double *d_g = d_h + (((size_t)n + 31) & ~size_t(31));
+    QEW_CUDA(ctx, cudaMemcpyAsync(d_h, h_h, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    QEW_TRY(qew_gradient_enqueue(ctx, field, d_h, n, p, precision, d_g));
+    QEW_CUDA(ctx, cudaMemcpyAsync(h_grad, d_g, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return QEW_OK;
+}
+
+}  // extern "C"

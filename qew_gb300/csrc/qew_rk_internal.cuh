@@ -1,0 +1,12 @@
+// qew_rk_internal.cuh -- Rosso-Krauth entry points shared between forms.
+#pragma once
+
+#include "qew_internal.cuh"
+
+qew_status qew_rk_validate(qew_ctx *ctx, int n, const qew_params *p, const qew_rk_params *rp);
+qew_status qew_rk_block_plain(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
+                              const qew_params *p, const qew_rk_params *rp, qew_rk_result *res);
+// Chooses the persistent form when available, else the host-driven one.
+qew_status qew_rk_block_dispatch(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
+                                 const qew_params *p, const qew_rk_params *rp,
+                                 qew_rk_result *res);

@@ -1,0 +1,141 @@
+"""Regenerate the golden fixtures of the qEW reference's own test suite.
+
+The reference pins its B-spline field and its L-BFGS against SciPy through two
+HDF5 fixtures made by tests/data/gen_golden.py and tests/data/gen_lbfgs_golden.py.
+h5py is not available here, so this script restates the same generator math
+with numpy/scipy and writes the arrays as ``.npz``:
+
+* ``noise_golden.npz`` -- a 64x48 band-limited field (Lx=3.2, Ly=1,
+  amplitude 1.7, xi 0.15, seed 7), SciPy's grid-wrap cubic-spline
+  coefficients, and value / finite-difference derivatives of the interpolant
+  at 256 query points in [-L, 2L) (reference gen_golden.py:22-56).
+* ``lbfgs_golden.npz`` -- a 48x32 field (Lx=2.4, amplitude 0.2, xi 0.25,
+  line tension 3, seed 4), the flat start h0 = 0.5, and the minimum energy of
+  SciPy's fmin_l_bfgs_b on the reference energy (reference
+  gen_lbfgs_golden.py:21-70).
+
+When the reference tree is present (``--reference DIR``, default the mounted
+copy) the script also checks that the regenerated arrays occur byte-for-byte
+in the reference's committed ``.h5`` files, and reads the committed ``e_min``
+attribute (a little-endian double at byte offset 1192 of lbfgs_golden.h5) so
+the fixture carries the reference's own number next to the recomputed one.
+
+Run:  python tests/golden/gen_golden.py
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import struct
+
+import numpy as np
+from scipy.ndimage import map_coordinates, spline_filter
+from scipy.optimize import fmin_l_bfgs_b
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+MODE = "grid-wrap"
+
+
+def band_limited_field(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed):
+    """Random-phase spectrum masked to the correlation ellipse, inverse FFT,
+    real part, scaled to the population std (gen_golden.py:31-38)."""
+    dx, dy = Lx / nx, Ly / ny
+    np.random.seed(seed)
+    fx = np.fft.fftfreq(nx) / dx
+    fy = np.fft.fftfreq(ny) / dy
+    FX, FY = np.meshgrid(fx, fy, indexing="ij")
+    A = np.exp(1j * np.random.uniform(0, 2 * np.pi, (nx, ny)))
+    A[(FX * xi_x) ** 2 + (FY * xi_y) ** 2 > 1] = 0
+    f = np.real(np.fft.ifft2(A))
+    f *= amplitude / np.std(f)
+    return f
+
+
+def noise_golden():
+    nx, ny, Lx, Ly, amp, xi, seed = 64, 48, 3.2, 1.0, 1.7, 0.15, 7
+    dx, dy = Lx / nx, Ly / ny
+    field = band_limited_field(nx, ny, Lx, Ly, amp, xi, xi, seed)
+    coef = spline_filter(field, order=3, mode=MODE)
+    rng = np.random.default_rng(123)
+    M = 256
+    xq = rng.uniform(-Lx, 2 * Lx, M)
+    yq = rng.uniform(-Ly, 2 * Ly, M)
+    gx = (xq / dx) % nx
+    gy = (yq / dy) % ny
+    hstep = 1e-4
+
+    def mc(a, b):
+        return map_coordinates(coef, [a, b], order=3, mode=MODE, prefilter=False)
+
+    v = mc(gx, gy)
+    dvdx = (mc((gx + hstep) % nx, gy) - mc((gx - hstep) % nx, gy)) / (2 * hstep) / dx
+    dvdy = (mc(gx, (gy + hstep) % ny) - mc(gx, (gy - hstep) % ny)) / (2 * hstep) / dy
+    return dict(nx=nx, ny=ny, Lx=Lx, Ly=Ly, amplitude=amp, xi=xi, field=field,
+                coef_scipy=coef, x=xq, y=yq, v=v, dvdx=dvdx, dvdy=dvdy)
+
+
+def lbfgs_golden():
+    nx, ny, Lx, Ly, amp, xi, lt, seed = 48, 32, 2.4, 1.0, 0.2, 0.25, 3.0, 4
+    dx, dy = Lx / nx, Ly / ny
+    field = band_limited_field(nx, ny, Lx, Ly, amp, xi, xi, seed)
+    coef = spline_filter(field, order=3, mode=MODE)
+    x = np.arange(nx) * dx
+
+    def objective(h):
+        dh = (np.roll(h, -1) - h) / dx
+        line_energy = lt * dh ** 2 / 2
+        xc = (np.roll(x, -1) + x) / 2
+        hc = (np.roll(h, -1) + h) / 2
+        gx = (xc / dx) % nx
+        gy = (hc / dy) % ny
+        v = map_coordinates(coef, [gx, gy], order=3, mode=MODE, prefilter=False)
+        return float(np.sum(dx * (line_energy + v)))
+
+    h0 = np.full(nx, 0.5 * Ly)
+    h_min, e_min, info = fmin_l_bfgs_b(objective, h0, approx_grad=True, factr=10.0,
+                                       pgtol=1e-10, maxiter=20000)
+    return dict(nx=nx, ny=ny, Lx=Lx, Ly=Ly, amplitude=amp, xi=xi, line_tension=lt,
+                field=field, h0=h0, h_min_scipy=h_min, e_min_scipy=e_min)
+
+
+def check_against_reference(ref_dir, ng, lg):
+    """Byte-level cross-check against the reference's committed fixtures."""
+    out = {}
+    p = os.path.join(ref_dir, "tests", "data", "noise_golden.h5")
+    if os.path.exists(p):
+        blob = open(p, "rb").read()
+        for k in ("field", "x", "y", "v", "dvdx", "dvdy"):
+            out["noise_" + k] = np.ascontiguousarray(ng[k]).tobytes() in blob
+    p = os.path.join(ref_dir, "tests", "data", "lbfgs_golden.h5")
+    if os.path.exists(p):
+        blob = open(p, "rb").read()
+        out["lbfgs_field"] = np.ascontiguousarray(lg["field"]).tobytes() in blob
+        out["lbfgs_h0"] = np.ascontiguousarray(lg["h0"]).tobytes() in blob
+        e_ref = struct.unpack_from("<d", blob, 1192)[0]
+        # the attribute sits at a fixed offset of this exact file; accept it
+        # only if it is the minimum of the same problem to the test's tolerance
+        if abs(e_ref - lg["e_min_scipy"]) <= 1e-5 * abs(lg["e_min_scipy"]):
+            out["lbfgs_e_min_ref"] = e_ref
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    args = ap.parse_args()
+    ng = noise_golden()
+    lg = lbfgs_golden()
+    chk = check_against_reference(args.reference, ng, lg) if os.path.isdir(args.reference) else {}
+    print("reference cross-check:", chk if chk else "reference tree not present")
+    e_ref = chk.get("lbfgs_e_min_ref", np.nan)
+    verified = bool(chk) and all(v for k, v in chk.items() if k != "lbfgs_e_min_ref")
+    np.savez(os.path.join(HERE, "noise_golden.npz"), **ng,
+             verified_bytes=np.array(verified))
+    np.savez(os.path.join(HERE, "lbfgs_golden.npz"), **lg, e_min_ref=np.array(e_ref),
+             verified_bytes=np.array(verified))
+    print("wrote noise_golden.npz, lbfgs_golden.npz  e_min_scipy=%.17g e_min_ref=%.17g"
+          % (lg["e_min_scipy"], e_ref))
+
+
+if __name__ == "__main__":
+    main()

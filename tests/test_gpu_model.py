@@ -1,0 +1,164 @@
+"""GPU parity of the field, energy and gradient against the CPU oracle.
+
+Tolerance: FP64 results within 1e-12 relative (to the largest magnitude of the
+compared quantity), the bar stated for energy and gradient; the golden-vector
+checks use the reference's own tolerances.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import band_limited_field
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+PI = 3.14159265358979323846
+
+
+def t64(a):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def npy(t):
+    return t.detach().cpu().numpy()
+
+
+def close(a, b, rtol=RTOL):
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    err = float(np.max(np.abs(np.asarray(a) - np.asarray(b))))
+    assert err <= rtol * scale, "max err %.3e vs scale %.3e" % (err, scale)
+
+
+def fields(Q, O):
+    """(gpu noise, oracle noise) pairs for every field kind."""
+    nx, ny, Lx, Ly = 96, 40, 4.8, 1.3
+    fld = band_limited_field(nx, ny, Lx, Ly, 0.8, 0.3, 5)
+    g = Q.FilteredNoise(fld, Lx, Ly)
+    yield "bspline", g, O.BSplineField(fld, Lx, Ly, coef=g.coefficients())
+    yield "zero", Q.ZeroNoise(), O.ZeroNoise()
+    yield "const", Q.ConstNoise(0.7), O.ConstNoise(0.7)
+    yield "harmonic", Q.HarmonicWell(2.0, 0.5), O.HarmonicWell(2.0, 0.5)
+    yield "washboard", Q.SinusoidNoise(0.1, 2 * PI), O.SinusoidNoise(0.1, 2 * PI)
+    yield "sincos", Q.AnalyticNoise(0.3, 0.7, 1.3), O.AnalyticNoise(0.3, 0.7, 1.3)
+
+
+def test_prefilter_matches_oracle(Q, O):
+    for nx, ny, seed in [(64, 48, 1), (33, 17, 2), (1, 8, 3), (128, 1, 4), (7, 5, 5)]:
+        fld = np.random.default_rng(seed).standard_normal((nx, ny))
+        g = Q.FilteredNoise(fld, 2.0, 1.0).coefficients()
+        close(g, O.prefilter(fld), 1e-13)
+
+
+def test_sample_matches_golden_and_oracle(Q, O, noise_golden):
+    g = noise_golden
+    f = Q.FilteredNoise(g["field"], float(g["Lx"]), float(g["Ly"]))
+    v, dvdx, dvdy = (npy(t) for t in f.sample(g["x"], g["y"]))
+    assert np.max(np.abs(v - g["v"])) < 1e-7  # test_filtered_noise.cpp:319-323
+    assert np.max(np.abs(dvdx - g["dvdx"])) < 1e-4
+    assert np.max(np.abs(dvdy - g["dvdy"])) < 1e-4
+    of = O.BSplineField(g["field"], float(g["Lx"]), float(g["Ly"]))
+    ov, odx, ody = O.sample(of, g["x"], g["y"])
+    close(v, ov)
+    close(dvdx, odx)
+    close(dvdy, ody)
+
+
+def test_periodic_wrap_gpu(Q):
+    nx, ny, Lx, Ly = 48, 40, 2.5, 1.3
+    f = Q.FilteredNoise(band_limited_field(nx, ny, Lx, Ly, 1.0, 0.25, 17), Lx, Ly)
+    rng = np.random.default_rng(123)
+    x, y = rng.uniform(0, Lx, 60), rng.uniform(0, Ly, 60)
+    base = [npy(t) for t in f.sample(x, y)]
+    for sx, sy in [(1, 0), (0, 1), (-1, 0), (0, -1), (3, -2), (-5, 7), (-13, -11)]:
+        s = [npy(t) for t in f.sample(x + sx * Lx, y + sy * Ly)]
+        for a, b in zip(base, s):
+            assert np.max(np.abs(a - b)) < 1e-9
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 96, 257, 1000, 4096])
+@pytest.mark.parametrize("model", [0, 1])
+def test_gradient_objective_match_oracle(Q, O, n, model):
+    rng = np.random.default_rng(n * 7 + model)
+    h = rng.uniform(-0.6, 2.1, n)
+    for name, gq, go in fields(Q, O):
+        L = 4.8 if name == "bspline" else float(n)
+        pq = Q.Params(L, 1.3, 0.37, Q.Model(model))
+        po = O.params(L, 1.3, 0.37, model)
+        ht = t64(h)
+        close(npy(Q.gradient(ht, pq, gq)), O.gradient(h, po, go))
+        e_q, e_o = Q.objective(ht, pq, gq), O.objective(h, po, go)
+        assert abs(e_q - e_o) <= RTOL * max(abs(e_o), 1.0), (name, e_q, e_o)
+        d = rng.standard_normal(n)
+        et_q = Q.objective_trial(ht, t64(d), 0.3, pq, gq)
+        et_o = O.objective_trial(h, d, 0.3, po, go)
+        assert abs(et_q - et_o) <= RTOL * max(abs(et_o), 1.0), name
+
+
+def test_objective_is_reproducible(Q):
+    n = 100_000
+    f = Q.FilteredNoise(band_limited_field(256, 64, 25.6, 1.0, 1.0, 0.3, 9), 25.6, 1.0)
+    h = t64(np.random.default_rng(1).uniform(0, 1, n))
+    p = Q.Params(25.6, 1.0, 0.2, Q.Model.Arclength)
+    vals = {Q.objective(h, p, f) for _ in range(5)}
+    assert len(vals) == 1
+
+
+def test_known_answers_gpu(Q):
+    """test_qew_model.cpp:110-163 on the GPU."""
+    n, L, c, v0, fdr = 50, 3.0, 0.7, 1.25, 0.4
+    for model in (Q.Model.Linear, Q.Model.Arclength):
+        e = Q.objective(t64(np.full(n, c)), Q.Params(L, 2.3, fdr, model), Q.ConstNoise(v0))
+        assert abs(e - L * (v0 - fdr * c)) < 1e-12
+    n, lt, a = 32, 1.7, 0.9
+    h = a * np.sin(2 * PI * np.arange(n) / n)
+    e = Q.objective(t64(h), Q.Params(float(n), lt, 0.0, Q.Model.Linear), Q.ConstNoise(0.0))
+    assert abs(e - (lt * a * a * n / 2) * (1 - np.cos(2 * PI / n))) < 1e-10
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_gradient_fd_consistency_gpu(Q, model):
+    """test_filtered_noise.cpp:187-230 on the GPU (tolerance 1e-5)."""
+    nx, ny, Lx, Ly = 64, 64, 3.2, 1.0
+    f = Q.FilteredNoise(band_limited_field(nx, ny, Lx, Ly, 0.5, 0.3, 11), Lx, Ly)
+    p = Q.Params(Lx, 0.5, 0.1, Q.Model(model))
+    h = np.random.default_rng(7).uniform(0.2, 0.8, nx)
+    g = npy(Q.gradient(t64(h), p, f))
+    eps = 1e-6
+    fd = np.empty(nx)
+    for j in range(nx):
+        hp, hm = h.copy(), h.copy()
+        hp[j] += eps
+        hm[j] -= eps
+        fd[j] = (Q.objective(t64(hp), p, f) - Q.objective(t64(hm), p, f)) / (2 * eps)
+    assert np.max(np.abs(fd - g)) < 1e-5
+
+
+def test_gradient_full_size_line(Q, O):
+    """A 2^20-point line on a 2^20 x 64 field: the whole gradient against the
+    oracle evaluated on the same (downloaded) coefficients."""
+    import torch
+    n, ny = 1 << 20, 64
+    rng = np.random.default_rng(5)
+    fld = rng.standard_normal((n, ny))
+    f = Q.FilteredNoise(fld, float(n), float(ny))
+    coef = f.coefficients()
+    of = O.BSplineField(fld, float(n), float(ny), coef=coef)
+    h = 32 + np.cumsum(rng.standard_normal(n)) * 0.05
+    for model in (0, 1):
+        p = Q.Params(float(n), 1.0, 0.3, Q.Model(model))
+        g = npy(Q.gradient(t64(h), p, f))
+        close(g, O.gradient(h, O.params(float(n), 1.0, 0.3, model), of, omp=True))
+    del f
+    torch.cuda.empty_cache()
+
+
+def test_gradient_host_roundtrip(Q, O):
+    n = 5000
+    f = Q.FilteredNoise(band_limited_field(500, 32, 50.0, 1.0, 1.0, 0.5, 3), 50.0, 1.0)
+    h = np.random.default_rng(2).uniform(0, 1, n)
+    p = Q.Params(50.0, 1.0, 0.1, Q.Model.Linear)
+    g_host = Q.gradient_host(h, p, f)
+    g_dev = npy(Q.gradient(t64(h), p, f))
+    assert np.array_equal(g_host, g_dev)

@@ -1,0 +1,213 @@
+"""CPU oracle pinned against the reference's golden vectors and known answers.
+
+Every case here restates a test of the reference suite (file:line in each
+docstring), with the reference's tolerance, against the oracle. The GPU tests
+then compare the CUDA path with this oracle.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import band_limited_field
+
+PI = 3.14159265358979323846
+
+
+def test_prefilter_matches_scipy_grid_wrap(O, noise_golden):
+    """The FFT prefilter equals SciPy's spline_filter(mode='grid-wrap')
+    (filtered_noise.h:59-62; gen_golden.py:40)."""
+    coef = O.prefilter(noise_golden["field"])
+    assert np.max(np.abs(coef - noise_golden["coef_scipy"])) < 1e-12
+
+
+def test_sample_matches_scipy_golden(O, noise_golden):
+    """test_filtered_noise.cpp:286-324: value 1e-7, derivatives 1e-4."""
+    g = noise_golden
+    assert bool(g["verified_bytes"]), "fixture not byte-verified against the reference"
+    f = O.BSplineField(g["field"], float(g["Lx"]), float(g["Ly"]))
+    v, dvdx, dvdy = O.sample(f, g["x"], g["y"])
+    assert np.max(np.abs(v - g["v"])) < 1e-7
+    assert np.max(np.abs(dvdx - g["dvdx"])) < 1e-4
+    assert np.max(np.abs(dvdy - g["dvdy"])) < 1e-4
+
+
+def test_lbfgs_matches_scipy_golden(O, lbfgs_golden):
+    """test_lbfgs.cpp:309-349: preconditioned, ftol 1e-8, e within 1e-5 rel of
+    the reference's committed SciPy minimum."""
+    g = lbfgs_golden
+    f = O.BSplineField(g["field"], float(g["Lx"]), float(g["Ly"]))
+    p = O.params(float(g["Lx"]), float(g["line_tension"]), 0.0, 0)
+    h = g["h0"].copy()
+    r = O.lbfgs_minimize(h, p, f, O.lbfgs_default_params(ftol=1e-8, precondition=1))
+    assert r.converged
+    e = O.objective(h, p, f)
+    e_ref = float(g["e_min_ref"])
+    assert np.isfinite(e_ref)
+    assert abs(e - e_ref) <= 1e-5 * abs(e_ref) + 1e-6
+
+
+def test_nodes_reproduced(O):
+    """test_filtered_noise.cpp:118-143."""
+    nx, ny, Lx, Ly = 64, 48, 3.2, 1.0
+    field = band_limited_field(nx, ny, Lx, Ly, 1.5, 0.15, 3)
+    f = O.BSplineField(field, Lx, Ly)
+    ii, jj = np.meshgrid(np.arange(0, nx, 5), np.arange(0, ny, 5), indexing="ij")
+    v, _, _ = O.sample(f, ii.ravel() * (Lx / nx), jj.ravel() * (Ly / ny))
+    assert np.max(np.abs(v - field[ii.ravel(), jj.ravel()])) < 1e-9
+
+
+def test_periodic_wrap(O):
+    """test_filtered_noise.cpp:238-281: shifts by whole periods are exact."""
+    nx, ny, Lx, Ly = 48, 40, 2.5, 1.3
+    f = O.BSplineField(band_limited_field(nx, ny, Lx, Ly, 1.0, 0.25, 17), Lx, Ly)
+    rng = np.random.default_rng(123)
+    x, y = rng.uniform(0, Lx, 60), rng.uniform(0, Ly, 60)
+    base = O.sample(f, x, y)
+    for sx, sy in [(1, 0), (0, 1), (-1, 0), (0, -1), (3, -2), (-5, 7), (-13, -11)]:
+        s = O.sample(f, x + sx * Lx, y + sy * Ly)
+        for a, b in zip(base, s):
+            assert np.max(np.abs(a - b)) < 1e-9
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_gradient_matches_fd_analytic(O, model):
+    """test_qew_model.cpp:44-100 (AnalyticNoise, tolerance 1e-6)."""
+    n = 64
+    p = O.params(float(n), 1.0, 0.37, model)
+    nz = O.AnalyticNoise()
+    h = np.random.default_rng(12345).uniform(0, 1, n)
+    g = O.gradient(h, p, nz)
+    eps = 1e-6
+    fd = np.empty(n)
+    for j in range(n):
+        hp, hm = h.copy(), h.copy()
+        hp[j] += eps
+        hm[j] -= eps
+        fd[j] = (O.objective(hp, p, nz) - O.objective(hm, p, nz)) / (2 * eps)
+    assert np.max(np.abs(fd - g)) < 1e-6
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_gradient_matches_fd_bspline(O, model):
+    """test_filtered_noise.cpp:187-230 (real field, tolerance 1e-5)."""
+    nx, ny, Lx, Ly = 64, 64, 3.2, 1.0
+    f = O.BSplineField(band_limited_field(nx, ny, Lx, Ly, 0.5, 0.3, 11), Lx, Ly)
+    p = O.params(Lx, 0.5, 0.1, model)
+    h = np.random.default_rng(7).uniform(0.2 * Ly, 0.8 * Ly, nx)
+    g = O.gradient(h, p, f)
+    eps = 1e-6
+    fd = np.empty(nx)
+    for j in range(nx):
+        hp, hm = h.copy(), h.copy()
+        hp[j] += eps
+        hm[j] -= eps
+        fd[j] = (O.objective(hp, p, f) - O.objective(hm, p, f)) / (2 * eps)
+    assert np.max(np.abs(fd - g)) < 1e-5
+
+
+def test_flat_line_energy(O):
+    """test_qew_model.cpp:110-132: E = L (v0 - f c) to 1e-12."""
+    n, L, c, v0, fdr = 50, 3.0, 0.7, 1.25, 0.4
+    for model in (0, 1):
+        e = O.objective(np.full(n, c), O.params(L, 2.3, fdr, model), O.ConstNoise(v0))
+        assert abs(e - L * (v0 - fdr * c)) < 1e-12
+
+
+def test_sinusoid_linear_energy(O):
+    """test_qew_model.cpp:140-163: closed-form discrete elastic energy."""
+    n, lt, a = 32, 1.7, 0.9
+    h = a * np.sin(2 * PI * np.arange(n) / n)
+    e = O.objective(h, O.params(float(n), lt, 0.0, 0), O.ConstNoise(0.0))
+    assert abs(e - (lt * a * a * n / 2) * (1 - np.cos(2 * PI / n))) < 1e-10
+
+
+def test_precond_matches_numpy_fft(O):
+    """The preconditioner is irfft(rfft(q)/eig) with kokkos-fft normalisation
+    (lbfgs.h:117-118, 138-145, 173-180)."""
+    for n in (1, 2, 7, 64, 100, 1024):
+        q = np.random.default_rng(n).standard_normal(n)
+        d = O.precond_apply(q, 1.3, 5.0, 0.2)
+        k = np.arange(n // 2 + 1)
+        eig = (1.3 / (5.0 / n)) * 4 * np.sin(PI * k / n) ** 2 + 0.2
+        ref = np.fft.irfft(np.fft.rfft(q) / eig, n)
+        assert np.max(np.abs(d - ref)) < 1e-12 * max(1.0, np.max(np.abs(ref)))
+
+
+def test_lbfgs_reference_cases(O):
+    """test_lbfgs.cpp:68-124, 128-141, 150-188: flat relaxation, harmonic
+    minimum (both models), non-convergence flag, curvature skip, LS give-up."""
+    n = 128
+    h = 0.5 + 0.3 * np.cos(4 * PI * np.arange(n) / n)
+    r = O.lbfgs_minimize(h, O.params(float(n), 1.0, 0.0, 0), O.ZeroNoise(),
+                         O.lbfgs_default_params(ftol=1e-9))
+    assert r.converged and np.ptp(h) < 1e-6
+    for model in (0, 1):
+        h = np.zeros(96)
+        r = O.lbfgs_minimize(h, O.params(96.0, 1.0, 0.0, model), O.HarmonicWell(2.0, 0.5),
+                             O.lbfgs_default_params(ftol=1e-9))
+        assert r.converged and np.max(np.abs(h - 0.5)) < 1e-6
+    h = np.zeros(96)
+    r = O.lbfgs_minimize(h, O.params(96.0, 1.0, 0.0, 0), O.HarmonicWell(2.0, 0.5),
+                         O.lbfgs_default_params(ftol=1e-12, max_iter=1))
+    assert not r.converged and r.max_force >= 1e-12
+    h = np.zeros(16)
+    r = O.lbfgs_minimize(h, O.params(16.0, 1.0, 0.0, 0), O.HarmonicWell(2.0, 0.5),
+                         O.lbfgs_default_params(ftol=1e-8, max_iter=20000, curvature_eps=1e30))
+    assert r.n_curvature_skips > 0 and r.converged and np.max(np.abs(h - 0.5)) < 1e-6
+    h = np.zeros(32)
+    r = O.lbfgs_minimize(h, O.params(32.0, 1.0, 0.0, 0), O.HarmonicWell(2.0, 0.5),
+                         O.lbfgs_default_params(ftol=1e-9, max_ls=0))
+    assert not r.converged and r.iterations == 0 and r.n_ls_restarts == 0
+
+
+def test_rk_washboard_fc(O):
+    """test_rosso_krauth.cpp:51-89: f_c = A k recovered by bisection to 2%."""
+    n, A, k = 16, 0.1, 2 * PI
+    lam = 2 * PI / k
+    nz = O.SinusoidNoise(A, k)
+    rp = O.rk_params(lam / 200, lam, 1e-12, 1e-11, 3 * lam, 100000)
+
+    def blocks(f):
+        return O.rk_block(np.zeros(n), O.params(float(n), 1.0, f, 0), nz, rp).blocked
+
+    lo, hi = 0.0, 2 * A * k
+    assert blocks(lo) and not blocks(hi)
+    for _ in range(40):
+        m = 0.5 * (lo + hi)
+        if blocks(m):
+            lo = m
+        else:
+            hi = m
+    assert abs(0.5 * (lo + hi) - A * k) < 0.02 * A * k
+
+
+def test_rk_velocity_is_minus_gradient(O):
+    """test_rosso_krauth.cpp:94-141: rk_site_velocity == -gradient to 1e-12."""
+    nx, ny, Lx, Ly = 64, 64, 3.2, 1.0
+    f = O.BSplineField(band_limited_field(nx, ny, Lx, Ly, 0.7, 0.2, 13), Lx, Ly)
+    h = np.random.default_rng(21).uniform(0.1 * Ly, 0.9 * Ly, nx)
+    for model in (0, 1):
+        p = O.params(Lx, 1.3, 0.4, model)
+        g = O.gradient(h, p, f)
+        dx = Lx / nx
+        v = np.array([O.rk_site_velocity(i, nx, dx, 1.3, 0.4, model, h[i], h[i - 1],
+                                         h[(i + 1) % nx], f) for i in range(nx)])
+        assert np.max(np.abs(v + g)) < 1e-12
+
+
+def test_rk_odd_length_rejected(O):
+    """test_rosso_krauth.cpp:296-313."""
+    with pytest.raises(ValueError):
+        O.rk_block(np.zeros(17), O.params(17.0, 1.0, 0.0, 0), O.SinusoidNoise(),
+                   O.rk_params(0.01, 1.0, 1e-10, 1e-9, 3.0))
+
+
+def test_philox_normals_moments(O):
+    """Philox4x32-10 + Box-Muller increments are N(0,1)."""
+    z = np.concatenate([O.philox_normals(1, s, 4096) for s in range(64)])
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
+    assert abs(np.mean(z ** 4) - 3.0) < 0.1
+    a, b = O.philox_normals(7, 3, 1000), O.philox_normals(7, 3, 1000)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, O.philox_normals(7, 4, 1000))
