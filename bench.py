@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32split"])
+    ap.add_argument("--precision", default="fp32split", choices=["fp64", "fp32split"])
     ap.add_argument("--small", action="store_true",
                     help="small case for profiling: L=2^20, 64-row field, one instance")
     ap.add_argument("--profile-run", action="store_true",
@@ -214,6 +214,21 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- our arm
+def timed(torch, fn, steps, ctx):
+    """Run fn() `steps` times between CUDA events on the current stream;
+    returns (elapsed ms, number of this library's kernel launches)."""
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    l0 = ctx.launches()
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), ctx.launches() - l0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -225,14 +240,12 @@ def run_ours(args):
     qbuild.build()
     import qew_gb300 as Q
 
-    prec = Q.QEW_PREC_FP64 if args.precision == "fp64" else Q.QEW_PREC_FP32_SPLIT
     if args.small:
         L, ny, n_inst = L_FULL, 64, 1
     else:
         L, ny, n_inst = L_FULL, NY_FULL, N_INST
-    store = Q.QEW_STORE_FP64 | (Q.QEW_STORE_FP32 if prec == Q.QEW_PREC_FP32_SPLIT else 0)
     field = gaussian_field_gpu(torch, L, ny, XI, SEED + rank)
-    noise = Q.FilteredNoise(field, float(L), float(ny), store=store)
+    noise = Q.FilteredNoise(field, float(L), float(ny), store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
     del field
     torch.cuda.empty_cache()
     rng = np.random.default_rng(SEED + 1000 * rank)
@@ -240,16 +253,26 @@ def run_ours(args):
     hs_host = [np.ascontiguousarray(band * (k + 0.5) + smooth_walk(rng, L, min(8.0, band / 8), 64.0))
                for k in range(n_inst)]
     hs = [torch.as_tensor(h, device="cuda") for h in hs_host]
-    gs = [torch.empty_like(h) for h in hs]
+    g64 = [torch.empty_like(h) for h in hs]
+    splits = [Q.split_heights(h, noise) for h in hs]
+    g32 = [torch.empty(L, dtype=torch.float32, device="cuda") for _ in hs]
     p = Q.Params(float(L), 1.0, 0.0, Q.Model.Linear)
     ctx = noise.ctx
 
-    def step():
+    def step_split():
         for k in range(n_inst):
-            Q.gradient(hs[k], p, noise, gs[k], precision=prec)
+            Q.gradient_split(splits[k][0], splits[k][1], p, noise, g32[k])
 
-    for _ in range(max(args.warmup, 3)):
-        step()
+    def step_fp64():
+        for k in range(n_inst):
+            Q.gradient(hs[k], p, noise, g64[k])
+
+    headline_split = args.precision == "fp32split"
+    step_main, step_other = (step_split, step_fp64) if headline_split else (step_fp64, step_split)
+    warm = max(args.warmup, 3)
+    for _ in range(warm):
+        step_main()
+        step_other()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     if not args.profile_run:
@@ -257,40 +280,35 @@ def run_ours(args):
         time.sleep(0.3)
     if ws > 1:
         torch.distributed.barrier()
-    torch.cuda.synchronize()
-    stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = ctx.launches()
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    launches = ctx.launches() - l0
-    t_ms = e0.elapsed_time(e1)
+    t_ms, launches = timed(torch, step_main, args.steps, ctx)
     if ws > 1:
         t = torch.tensor([t_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_ms = float(t.item())
         torch.distributed.barrier()
     clk = clocks.stop() if not args.profile_run else None
-    points = args.steps * n_inst * L
-    value = ws * points / (t_ms * 1e-3)
+    t2_ms, launches2 = timed(torch, step_other, args.steps, ctx)
+    value = ws * args.steps * n_inst * L / (t_ms * 1e-3)
+    value_other = ws * args.steps * n_inst * L / (t2_ms * 1e-3)
 
-    # roofline of the dominant kernel (the only kernel in the timed region)
-    bytes_per_point = 48.0 if prec == Q.QEW_PREC_FP64 else 32.0
-    launch_ms = t_ms / max(launches, 1)
-    achieved = bytes_per_point * L / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": None,
-            "kernel": "k_gradient" if prec == Q.QEW_PREC_FP64 else "k_gradient_split",
-            "bytes_per_point": bytes_per_point, "peak_source": peak_kind}
+
+    def roofline(ms, nl, bpp, name):
+        launch_ms = ms / max(nl, 1)
+        ach = bpp * L / (launch_ms * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "traffic": None, "kernel": name, "bytes_per_point": bpp,
+                "launch_us": launch_ms * 1e3, "peak_source": peak_kind}
+
+    roof_split = roofline(t_ms if headline_split else t2_ms,
+                          launches if headline_split else launches2, 28.0, "k_gradient_split")
+    roof_fp64 = roofline(t2_ms if headline_split else t_ms,
+                         launches2 if headline_split else launches, 48.0, "k_gradient")
 
     e2e = None
     cpu = None
     if not args.profile_run:
-        # end to end through the C ABI with pinned host buffers
+        prec = Q.QEW_PREC_FP32_SPLIT if headline_split else Q.QEW_PREC_FP64
         hh = [torch.as_tensor(h).pin_memory().numpy() for h in hs_host]
         gh = [torch.empty(L, dtype=torch.float64).pin_memory().numpy() for _ in range(n_inst)]
         for k in range(n_inst):
@@ -303,25 +321,29 @@ def run_ours(args):
                 Q.gradient_host(hh[k], p, noise, gh[k], precision=prec)
         dt = time.perf_counter() - t0
         e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
-               "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8}
+               "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
+               "call": "qew_gradient_host (FP64 host heights in, FP64 host gradient out)"}
         if rank == 0 and args.cpu_seconds > 0:
             cpu = cpu_gradient_rate(args.cpu_seconds)
 
     if rank == 0:
+        other = {"precision": "fp64" if headline_split else "fp32split", "value": value_other,
+                 "unit": UNIT, "ms_per_step": t2_ms / args.steps,
+                 "roofline": roof_fp64 if headline_split else roof_split}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-                "steps": args.steps, "warmup": max(args.warmup, 3),
-                "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64" if prec == Q.QEW_PREC_FP64 else "f32",
-                "data": "synthetic",
+                "steps": args.steps, "warmup": warm, "ms_per_step": t_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if headline_split else "f64", "data": "synthetic",
                 "config": {"workload": "gradient of %d line instances of L=2^20 points on a "
                                        "2^20x%d field (xi=4 cells), %s gather"
                                        % (n_inst, ny, args.precision),
                            "L": L, "rows": ny, "instances_per_step": n_inst,
-                           "model": "linear", "l2": "inputs larger than L2 (8 disjoint row "
-                                                   "bands per step)",
+                           "model": "linear",
+                           "l2": "inputs larger than L2 (8 disjoint row bands per step)",
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
-                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-                "gpu_launches": launches, "clocks": clk}
+                "roofline": roof_split if headline_split else roof_fp64,
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+                "other_precision": other}
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

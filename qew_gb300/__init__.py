@@ -41,7 +41,7 @@ from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # n
 __all__ = [
     "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
     "SinusoidNoise", "AnalyticNoise", "objective", "objective_trial", "gradient",
-    "gradient_host", "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "precond_apply",
+    "gradient_host", "split_heights", "join_heights", "gradient_split", "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
     "depinning_bisect", "Context", "default_context", "QewError",
 ]
@@ -335,6 +335,47 @@ def gradient_host(h: np.ndarray, p: Params, noise: _Noise, out: np.ndarray | Non
                                           C.byref(pc), precision, C.c_void_p(out.ctypes.data)),
                 ctx.h, "gradient_host")
     return out
+
+
+def split_heights(h, noise: "FilteredNoise"):
+    """FP64 heights -> (int32 cell, float32 fraction) in field y-cells."""
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    cell = torch.empty(h.numel(), dtype=torch.int32, device="cuda")
+    frac = torch.empty(h.numel(), dtype=torch.float32, device="cuda")
+    _capi.check(ctx.lib.qew_split_heights(ctx.h, noise.h, _ptr(h), h.numel(),
+                                          C.c_void_p(cell.data_ptr()),
+                                          C.c_void_p(frac.data_ptr())), ctx.h, "split_heights")
+    return cell, frac
+
+
+def join_heights(cell, frac, noise: "FilteredNoise"):
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    h = torch.empty(cell.numel(), dtype=torch.float64, device="cuda")
+    _capi.check(ctx.lib.qew_join_heights(ctx.h, noise.h, C.c_void_p(cell.data_ptr()),
+                                         C.c_void_p(frac.data_ptr()), cell.numel(), _ptr(h)),
+                ctx.h, "join_heights")
+    return h
+
+
+def gradient_split(cell, frac, p: Params, noise: "FilteredNoise", grad=None):
+    """gradient() on split heights with FP32 output (the bandwidth form)."""
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    if cell.dtype != torch.int32 or frac.dtype != torch.float32:
+        raise ValueError("expected int32 cells and float32 fractions")
+    if grad is None:
+        grad = torch.empty(cell.numel(), dtype=torch.float32, device="cuda")
+    pc = p.c()
+    _capi.check(ctx.lib.qew_gradient_split(ctx.h, noise.h, C.c_void_p(cell.data_ptr()),
+                                           C.c_void_p(frac.data_ptr()), cell.numel(),
+                                           C.byref(pc), C.c_void_p(grad.data_ptr())),
+                ctx.h, "gradient_split")
+    return grad
 
 
 # ----------------------------------------------------------------- L-BFGS

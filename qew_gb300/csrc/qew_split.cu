@@ -1,9 +1,256 @@
-// qew_split.cu -- FP32 split-index gather (placeholder until implemented).
+// qew_split.cu -- FP32 split-index gather: the bandwidth form of gradient().
+//
+// Same algorithm as the FP64 gradient (qew_model.h:149-193, fused into one
+// kernel), with
+//   * an FP32 copy of the x-fastest B-spline coefficients (4 B per tap),
+//   * heights carried as an integer cell index plus an FP32 fraction in field
+//     y-cells, h = (cell + frac) * dy, so no FP64 arithmetic is needed: the
+//     edge midpoint (h_i + h_ip)/2 and the elastic differences are formed from
+//     exact integer cell sums plus FP32 fraction sums,
+//   * edge x positions from integer arithmetic when the line and the field
+//     share their resolution and length (gx = e + 1/2 exactly), FP64 only in
+//     the general case.
+// Error against the FP64 form is FP32 rounding of the field, weights and sums
+// (about 1e-6 of the gradient's scale; the tests state the bound).
+#include <cmath>
+
 #include "qew_internal.cuh"
 #include "qew_model_kernels.cuh"
+#include "qew_split.cuh"
 
-qew_status qew_gradient_split_enqueue(qew_ctx *ctx, const qew_field *field, const double *d_h,
-                                      int n, const qew_params *p, double *d_grad) {
-    (void)field; (void)d_h; (void)n; (void)p; (void)d_grad;
-    return qew_fail(ctx, QEW_ERR_UNSUPPORTED, "FP32 split gather not built yet");
+namespace {
+
+constexpr int kBS = 256;
+
+__device__ __forceinline__ void bsw_value_f(float t, float w[4]) {
+    const float s6 = 1.0f / 6.0f;
+    const float t2 = t * t, t3 = t2 * t, omt = 1.0f - t;
+    w[0] = omt * omt * omt * s6;
+    w[1] = (4.0f - 6.0f * t2 + 3.0f * t3) * s6;
+    w[2] = (1.0f + 3.0f * t + 3.0f * t2 - 3.0f * t3) * s6;
+    w[3] = t3 * s6;
 }
+__device__ __forceinline__ void bsw_deriv_f(float t, float dw[4]) {
+    const float t2 = t * t, omt = 1.0f - t;
+    dw[0] = -0.5f * omt * omt;
+    dw[1] = -2.0f * t + 1.5f * t2;
+    dw[2] = 0.5f + t - 1.5f * t2;
+    dw[3] = 0.5f * t2;
+}
+
+__device__ __forceinline__ int wrap_cell(int c, int n) {
+    if ((unsigned)c >= (unsigned)n) {
+        c %= n;
+        if (c < 0) c += n;
+    }
+    return c;
+}
+
+// x cell and fraction of the midpoint of edge (e, e+1 mod n).
+__device__ __forceinline__ void edge_x(const SplitGeom &g, int e, int &ix, float &fx) {
+    if (g.same_grid) {  // n == nx and P == Lx: gx = e + 1/2, wrap edge (n-1)/2
+        if (e + 1 < g.n) {
+            ix = e;
+            fx = 0.5f;
+        } else {
+            ix = (g.n - 1) >> 1;
+            fx = ((g.n - 1) & 1) ? 0.5f : 0.0f;
+        }
+        return;
+    }
+    const int ep = (e + 1 == g.n) ? 0 : e + 1;
+    double gx = (double)(e + ep) * g.half_ratio;
+    const double nd = (double)g.nx;
+    if (!(gx >= 0.0 && gx < nd)) gx -= floor(gx / nd) * nd;
+    int c = (int)floor(gx);
+    if (c >= g.nx) {
+        c -= g.nx;
+        gx -= nd;
+    }
+    fx = (float)(gx - (double)c);
+    ix = min(max(c, 0), g.nx - 1);
+}
+
+// dV/dy at (ix + fx, cy + fy) cells on FP32 coefficients.
+__device__ __forceinline__ float split_dvdy(const float *__restrict__ coef, int nx, int ny, int ix,
+                                            float fx, int cy, float fy, float inv_dy) {
+    int xs[4], ys[4];
+    wrap4(ix, nx, xs);
+    wrap4(wrap_cell(cy, ny), ny, ys);
+    float wx[4], dwy[4];
+    bsw_value_f(fx, wx);
+    bsw_deriv_f(fy, dwy);
+    float dg = 0.0f;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const float *row = coef + (size_t)ys[b] * (size_t)nx;
+        const float r = wx[0] * __ldg(row + xs[0]) + wx[1] * __ldg(row + xs[1]) +
+                        wx[2] * __ldg(row + xs[2]) + wx[3] * __ldg(row + xs[3]);
+        dg += dwy[b] * r;
+    }
+    return dg * inv_dy;
+}
+
+// Midpoint of two split heights: (c0 + f0 + c1 + f1) / 2 as (cell, frac).
+__device__ __forceinline__ void split_mid(int c0, float f0, int c1, float f1, int &cm, float &fm) {
+    const int C = c0 + c1;
+    float F = f0 + f1;       // [0, 2)
+    cm = C >> 1;             // floor(C / 2)
+    if (C & 1) F += 1.0f;    // odd sum: carry half a cell
+    fm = 0.5f * F;           // [0, 1.5)
+    if (fm >= 1.0f) {
+        fm -= 1.0f;
+        cm += 1;
+    }
+}
+
+template <bool IN64, bool OUT64>
+__global__ void __launch_bounds__(kBS)
+k_gradient_split(const double *__restrict__ h64, const int *__restrict__ hc,
+                 const float *__restrict__ hf, SplitGeom g, double *__restrict__ grad64,
+                 float *__restrict__ grad32) {
+    __shared__ int s_c[kBS + 2];
+    __shared__ float s_f[kBS + 2];
+    __shared__ float s_dv[kBS + 1];
+    __shared__ float s_sl[kBS + 1];
+    const int n = g.n;
+    const int base = blockIdx.x * kBS;
+    const int t = threadIdx.x;
+    const int i = base + t;
+    const int cnt = min(kBS, n - base);
+    auto load = [&](int site, int slot) {
+        if (IN64) {
+            const double y = h64[site];
+            const double gy = g.dy_pow2 ? y * g.inv_dy : y / g.dy;
+            const double fl = floor(gy);
+            s_c[slot] = (int)fl;
+            s_f[slot] = (float)(gy - fl);
+        } else {
+            s_c[slot] = hc[site];
+            s_f[slot] = hf[site];
+        }
+    };
+    if (t < cnt) load(i, t + 1);
+    if (t == 0) load(base == 0 ? n - 1 : base - 1, 0);
+    if (t == cnt - 1) load((i + 1 == n) ? 0 : i + 1, cnt + 1);
+    __syncthreads();
+    const bool arc = g.arc;
+    auto edge = [&](int e, int sl, int sr, int out) {
+        int ix, cm;
+        float fx, fm;
+        edge_x(g, e, ix, fx);
+        split_mid(s_c[sl], s_f[sl], s_c[sr], s_f[sr], cm, fm);
+        s_dv[out] = split_dvdy(g.coef, g.nx, g.ny, ix, fx, cm, fm, g.inv_dy_f);
+        if (arc) {
+            const float dh = ((float)(s_c[sr] - s_c[sl]) + (s_f[sr] - s_f[sl])) * g.dy_over_dx;
+            s_sl[out] = dh * rsqrtf(1.0f + dh * dh);
+        }
+    };
+    if (t < cnt) edge(i, t + 1, t + 2, t + 1);
+    if (t == 0) edge(base == 0 ? n - 1 : base - 1, 0, 1, 0);
+    __syncthreads();
+    if (t >= cnt) return;
+    float line_force;
+    if (!arc) {
+        const float d2 = (float)(s_c[t] + s_c[t + 2] - 2 * s_c[t + 1]) +
+                         (s_f[t] + s_f[t + 2] - 2.0f * s_f[t + 1]);
+        line_force = -g.lt_dy_over_dx2 * d2;
+    } else {
+        line_force = g.lt_over_dx * (s_sl[t] - s_sl[t + 1]);
+    }
+    const float gr = g.dx_f * (line_force + 0.5f * (s_dv[t] + s_dv[t + 1]) - g.f);
+    if (OUT64)
+        grad64[i] = (double)gr;
+    else
+        grad32[i] = gr;
+}
+
+__global__ void k_split_heights(const double *__restrict__ h, int n, double dy, double inv_dy,
+                                int dy_pow2, int *__restrict__ cell, float *__restrict__ frac) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double gy = dy_pow2 ? h[i] * inv_dy : h[i] / dy;
+    const double fl = floor(gy);
+    cell[i] = (int)fl;
+    frac[i] = (float)(gy - fl);
+}
+
+__global__ void k_join_heights(const int *__restrict__ cell, const float *__restrict__ frac, int n,
+                               double dy, double *__restrict__ h) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) h[i] = ((double)cell[i] + (double)frac[i]) * dy;
+}
+
+}  // namespace
+
+SplitGeom qew_split_geom(const qew_field *f, int n, const qew_params *p) {
+    SplitGeom g{};
+    g.coef = f->coef32;
+    g.n = n;
+    g.nx = f->nx;
+    g.ny = f->ny;
+    g.same_grid = (n == f->nx && p->physical_size == f->Lx) ? 1 : 0;
+    g.half_ratio = 0.5 * (p->physical_size / n) / f->dx;
+    g.dy = f->dy;
+    g.inv_dy = 1.0 / f->dy;
+    g.dy_pow2 = qew_is_pow2(f->dy) ? 1 : 0;
+    const double dx = p->physical_size / n;
+    g.inv_dy_f = (float)(1.0 / f->dy);
+    g.dy_over_dx = (float)(f->dy / dx);
+    g.lt_dy_over_dx2 = (float)(p->line_tension * f->dy / (dx * dx));
+    g.lt_over_dx = (float)(p->line_tension / dx);
+    g.dx_f = (float)dx;
+    g.f = (float)p->driving_force;
+    g.arc = (p->model == QEW_MODEL_ARCLENGTH) ? 1 : 0;
+    return g;
+}
+
+static qew_status split_check(qew_ctx *ctx, const qew_field *f, int n, const qew_params *p) {
+    if (!ctx || !f || !p || n < 1)
+        return qew_fail(ctx, QEW_ERR_INVALID, "split gradient: bad arguments");
+    if (f->kind != QEW_FIELD_BSPLINE || !f->coef32)
+        return qew_fail(ctx, QEW_ERR_INVALID,
+                        "split gradient: needs a B-spline field stored with QEW_STORE_FP32");
+    return QEW_OK;
+}
+
+qew_status qew_gradient_split_enqueue(qew_ctx *ctx, const qew_field *f, const double *d_h, int n,
+                                      const qew_params *p, double *d_grad) {
+    QEW_TRY(split_check(ctx, f, n, p));
+    const SplitGeom g = qew_split_geom(f, n, p);
+    k_gradient_split<true, true><<<(n + kBS - 1) / kBS, kBS, 0, ctx->stream>>>(
+        d_h, nullptr, nullptr, g, d_grad, nullptr);
+    return qew_launch_check(ctx, "gradient_split64");
+}
+
+extern "C" {
+
+qew_status qew_split_heights(qew_ctx *ctx, const qew_field *f, const double *d_h, int n,
+                             int32_t *d_cell, float *d_frac) {
+    if (!ctx || !f || !d_h || !d_cell || !d_frac || n < 1 || f->kind != QEW_FIELD_BSPLINE)
+        return qew_fail(ctx, QEW_ERR_INVALID, "split_heights: bad arguments");
+    k_split_heights<<<(n + 255) / 256, 256, 0, ctx->stream>>>(
+        d_h, n, f->dy, 1.0 / f->dy, qew_is_pow2(f->dy) ? 1 : 0, d_cell, d_frac);
+    return qew_launch_check(ctx, "split_heights");
+}
+
+qew_status qew_join_heights(qew_ctx *ctx, const qew_field *f, const int32_t *d_cell,
+                            const float *d_frac, int n, double *d_h) {
+    if (!ctx || !f || !d_h || !d_cell || !d_frac || n < 1 || f->kind != QEW_FIELD_BSPLINE)
+        return qew_fail(ctx, QEW_ERR_INVALID, "join_heights: bad arguments");
+    k_join_heights<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d_cell, d_frac, n, f->dy, d_h);
+    return qew_launch_check(ctx, "join_heights");
+}
+
+qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *f, const int32_t *d_cell,
+                              const float *d_frac, int n, const qew_params *p, float *d_grad) {
+    QEW_TRY(split_check(ctx, f, n, p));
+    if (!d_cell || !d_frac || !d_grad)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split: null buffer");
+    const SplitGeom g = qew_split_geom(f, n, p);
+    k_gradient_split<false, false><<<(n + kBS - 1) / kBS, kBS, 0, ctx->stream>>>(
+        nullptr, d_cell, d_frac, g, nullptr, d_grad);
+    return qew_launch_check(ctx, "gradient_split");
+}
+
+}  // extern "C"

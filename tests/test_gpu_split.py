@@ -1,0 +1,94 @@
+"""FP32 split-index gather against the FP64 oracle.
+
+Stated error of the precision change (gradient): max |g_split - g_fp64| <=
+2e-6 * (the largest term magnitude of the gradient, dx * (|F_el| + |dV/dy| +
+|f|)), from FP32 coefficients, weights and sums.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import band_limited_field, gaussian_field
+
+pytestmark = pytest.mark.gpu
+TOL = 2e-6
+
+
+def t64(a):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def npy(t):
+    return t.detach().cpu().numpy()
+
+
+def term_scale(O, h, po, of):
+    """Largest magnitude among the gradient's terms (elastic, pinning, force)."""
+    g_el = O.gradient(h, po, O.ZeroNoise())      # elastic + force only
+    g = O.gradient(h, po, of)
+    return max(np.max(np.abs(g_el)), np.max(np.abs(g - g_el)), 1e-300)
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("shape", [(1024, 64, 1024), (1000, 48, 1000), (777, 40, 500),
+                                   (300, 32, 901)])
+def test_split_gradient_error_bound(Q, O, model, shape):
+    nx, ny, n = shape
+    Lx, Ly = float(nx), float(ny)
+    fld = gaussian_field(nx, ny, 3.0, nx + ny)
+    f = Q.FilteredNoise(fld, Lx, Ly, store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    of = O.BSplineField(fld, Lx, Ly, coef=f.coefficients())
+    rng = np.random.default_rng(n)
+    h = ny / 2 + np.cumsum(rng.standard_normal(n)) * 0.2
+    h -= np.linspace(0, h[-1] - h[0], n)  # keep it roughly periodic
+    p = Q.Params(Lx, 1.0, 0.2, Q.Model(model))
+    po = O.params(Lx, 1.0, 0.2, model)
+    go = O.gradient(h, po, of)
+    scale = term_scale(O, h, po, of)
+    g64 = npy(Q.gradient(t64(h), p, f, precision=Q.QEW_PREC_FP32_SPLIT))
+    assert np.max(np.abs(g64 - go)) <= TOL * scale
+    cell, frac = Q.split_heights(t64(h), f)
+    g32 = npy(Q.gradient_split(cell, frac, p, f)).astype(np.float64)
+    assert np.max(np.abs(g32 - go)) <= TOL * scale
+    assert np.array_equal(g32, g64)
+
+
+def test_split_join_roundtrip(Q):
+    n, ny = 4096, 64
+    f = Q.FilteredNoise(np.random.default_rng(0).standard_normal((n, ny)), float(n), 6.4,
+                        store=Q.QEW_STORE_FP32)
+    h = np.random.default_rng(1).uniform(-50, 50, n)
+    cell, frac = Q.split_heights(t64(h), f)
+    c, fr = npy(cell), npy(frac)
+    assert np.all((fr >= 0) & (fr < 1))
+    assert np.array_equal(c, np.floor(h / 0.1).astype(np.int32))
+    back = npy(Q.join_heights(cell, frac, f))
+    assert np.max(np.abs(back - h)) < 1e-6 * 0.1
+
+
+def test_split_full_size(Q, O):
+    """L = 2^20 on a 2^20 x 64 field against the OpenMP oracle."""
+    import torch
+    n, ny = 1 << 20, 64
+    fld = np.random.default_rng(3).standard_normal((n, ny))
+    f = Q.FilteredNoise(fld, float(n), float(ny), store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    of = O.BSplineField(fld, float(n), float(ny), coef=f.coefficients())
+    rng = np.random.default_rng(4)
+    h = 32 + np.cumsum(rng.standard_normal(n)) * 0.02
+    po = O.params(float(n), 1.0, 0.1, 0)
+    go = O.gradient(h, po, of, omp=True)
+    cell, frac = Q.split_heights(t64(h), f)
+    g = npy(Q.gradient_split(cell, frac, Q.Params(float(n), 1.0, 0.1), f)).astype(np.float64)
+    g_el = O.gradient(h, po, O.ZeroNoise(), omp=True)
+    scale = max(np.max(np.abs(g_el)), np.max(np.abs(go - g_el)))
+    assert np.max(np.abs(g - go)) <= TOL * scale
+    del f
+    torch.cuda.empty_cache()
+
+
+def test_split_needs_fp32_storage(Q):
+    f = Q.FilteredNoise(band_limited_field(64, 32, 3.2, 1.0, 1.0, 0.3, 1), 3.2, 1.0)
+    with pytest.raises(ValueError, match="FP32"):
+        Q.gradient(t64(np.zeros(64)), Q.Params(3.2), f, precision=Q.QEW_PREC_FP32_SPLIT)
