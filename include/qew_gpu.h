@@ -210,6 +210,26 @@ qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *field,
                               const int32_t *d_cell, const float *d_frac,
                               int n, const qew_params *p, float *d_grad);
 
+/* Line energy without device allocation. No counterpart in the reference:
+ * an addition for callers that cannot call cudaMalloc where they need the
+ * energy (cudaMalloc/cudaFree can synchronise the whole device, which a
+ * latency-bound serving loop cannot afford; a process whose device memory is
+ * fully reserved up front gets out-of-memory from any extra allocation).
+ * Same energy as qew_objective (within rounding of the reduction order),
+ * written to the device pointer d_out on cuda_stream (NULL = legacy default
+ * stream); returns once the work is enqueued. Its reduction scratch is a
+ * static device array of QEW_NOALLOC_MAX_N/256 partial sums (32 KB) that
+ * every GPU loading this library holds until exit; lines longer than
+ * QEW_NOALLOC_MAX_N edges return QEW_ERR_INVALID. The field's device must be
+ * the current device. The first call on each device looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture. All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+#define QEW_NOALLOC_MAX_N 1048576
+qew_status qew_objective_noalloc(const qew_field *field, const double *d_h,
+                                 int n, const qew_params *p, double *d_out,
+                                 void *cuda_stream);
+
 /* ----------------------------------------------------------------- L-BFGS */
 qew_status qew_lbfgs_default_params(qew_lbfgs_params *lp);
 /* lbfgs_minimize(h, p, noise, lp), lbfgs.h:94-287; relaxes d_h in place. */

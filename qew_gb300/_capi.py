@@ -29,6 +29,7 @@ QEW_FIELD_HARMONIC, QEW_FIELD_WASHBOARD, QEW_FIELD_SINCOS = 3, 4, 5
 QEW_STORE_FP64, QEW_STORE_FP32 = 1, 2
 QEW_PREC_FP64, QEW_PREC_FP32_SPLIT = 0, 1
 QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
+QEW_NOALLOC_MAX_N = 1048576
 
 
 class qew_params(C.Structure):
@@ -87,6 +88,7 @@ _SIGS = {
     "qew_split_heights": (I, [VP, VP, VP, I, VP, VP]),
     "qew_join_heights": (I, [VP, VP, VP, VP, I, VP]),
     "qew_gradient_split": (I, [VP, VP, VP, VP, I, C.POINTER(qew_params), VP]),
+    "qew_objective_noalloc": (I, [VP, VP, I, C.POINTER(qew_params), VP, VP]),
     "qew_lbfgs_default_params": (I, [C.POINTER(qew_lbfgs_params)]),
     "qew_lbfgs_minimize": (I, [VP, VP, VP, I, C.POINTER(qew_params),
                                C.POINTER(qew_lbfgs_params), C.POINTER(qew_lbfgs_result)]),

@@ -1,0 +1,88 @@
+// qew_noalloc.cu -- line energy without any device-memory allocation.
+//
+// qew_objective needs reduction scratch (one partial sum per CTA and a ticket
+// counter), which lives in a context created with cudaMalloc. Some callers
+// cannot make that call where they need the energy: cudaMalloc and cudaFree
+// may synchronise the whole device, which a latency-bound serving loop
+// running other streams cannot afford; and a process whose device memory is
+// entirely reserved up front (an HBM budget, or another framework's caching
+// allocator owning the device) gets out-of-memory from any extra cudaMalloc.
+// qew_objective_noalloc serves them: the scratch is a file-scope device array
+// that every GPU loading this library holds until the process exits, so the
+// entry point itself allocates nothing. The caller passes the inputs and a
+// device pointer for the result.
+//
+// Limits and sharing: one partial per CTA of 256 edges, at most
+// QEW_NOALLOC_MAX_N = 4096 * 256 = 2^20 edges; longer lines are rejected with
+// QEW_ERR_INVALID. All calls on a device share the one array and it keeps
+// the previous call's contents, so the ticket counter is cleared at the start
+// of every call (the partials are rewritten before they are read); calls that
+// overlap on the GPU (different streams, or host threads) race on the array
+// and must be serialised by the caller.
+#include <mutex>
+
+#include "qew_internal.cuh"
+#include "qew_model_kernels.cuh"
+
+namespace {
+
+constexpr int kNoAllocBS = 256;
+constexpr int kNoAllocMaxBlocks = QEW_NOALLOC_MAX_N / kNoAllocBS;  // 4096
+constexpr int kMaxDevices = 64;
+
+// [0, 4096): per-CTA partial sums; element 4096 holds the ticket counter.
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxBlocks + 32];
+
+std::mutex g_setup_mu;
+double *g_scratch_ptr[kMaxDevices] = {};
+
+// The array's name is only a host-side stand-in: its device address is looked
+// up once per device, with that device current, and passed to the kernel.
+qew_status scratch_address(int device, double **out) {
+    if (device < 0 || device >= kMaxDevices) return QEW_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    if (!g_scratch_ptr[device]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return QEW_ERR_CUDA;
+        }
+        g_scratch_ptr[device] = (double *)p;
+    }
+    *out = g_scratch_ptr[device];
+    return QEW_OK;
+}
+
+}  // namespace
+
+extern "C" qew_status qew_objective_noalloc(const qew_field *field, const double *d_h, int n,
+                                            const qew_params *p, double *d_out,
+                                            void *cuda_stream) {
+    if (!field || !d_h || !p || !d_out || n < 1) return QEW_ERR_INVALID;
+    if (n > QEW_NOALLOC_MAX_N) return QEW_ERR_INVALID;  // beyond the static scratch
+    int device = -1;
+    if (cudaGetDevice(&device) != cudaSuccess) {
+        cudaGetLastError();
+        return QEW_ERR_CUDA;
+    }
+    if (device != field->device) return QEW_ERR_INVALID;  // make the field's device current
+    double *scratch = nullptr;
+    QEW_TRY(scratch_address(device, &scratch));
+    double *partials = scratch;
+    unsigned int *counter = (unsigned int *)(scratch + kNoAllocMaxBlocks);
+    cudaStream_t stream = (cudaStream_t)cuda_stream;
+    if (cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream) != cudaSuccess) {
+        cudaGetLastError();
+        return QEW_ERR_CUDA;
+    }
+    const double dx = p->physical_size / (double)n;
+    const int blocks = (n + kNoAllocBS - 1) / kNoAllocBS;  // <= kNoAllocMaxBlocks
+    return qew_dispatch_noise(nullptr, field, [&](auto nz) -> qew_status {
+        k_objective<decltype(nz), LineAt, kNoAllocBS><<<blocks, kNoAllocBS, 0, stream>>>(
+            n, dx, p->line_tension, p->driving_force, p->model, nz, LineAt{d_h}, partials,
+            counter, d_out);
+        const cudaError_t e = cudaGetLastError();
+        return e == cudaSuccess ? QEW_OK : QEW_ERR_CUDA;
+    });
+}
