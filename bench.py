@@ -254,14 +254,18 @@ def run_ours(args):
                for k in range(n_inst)]
     hs = [torch.as_tensor(h, device="cuda") for h in hs_host]
     g64 = [torch.empty_like(h) for h in hs]
-    splits = [Q.split_heights(h, noise) for h in hs]
-    g32 = [torch.empty(L, dtype=torch.float32, device="cuda") for _ in hs]
+    cells = torch.empty((n_inst, L), dtype=torch.int32, device="cuda")
+    fracs = torch.empty((n_inst, L), dtype=torch.float32, device="cuda")
+    for k in range(n_inst):
+        c, fr = Q.split_heights(hs[k], noise)
+        cells[k].copy_(c)
+        fracs[k].copy_(fr)
+    g32 = torch.empty((n_inst, L), dtype=torch.float32, device="cuda")
     p = Q.Params(float(L), 1.0, 0.0, Q.Model.Linear)
     ctx = noise.ctx
 
-    def step_split():
-        for k in range(n_inst):
-            Q.gradient_split(splits[k][0], splits[k][1], p, noise, g32[k])
+    def step_split():  # all instances in one launch
+        Q.gradient_split_batch(cells, fracs, p, noise, g32)
 
     def step_fp64():
         for k in range(n_inst):
@@ -295,7 +299,8 @@ def run_ours(args):
 
     def roofline(ms, nl, bpp, name):
         launch_ms = ms / max(nl, 1)
-        ach = bpp * L / (launch_ms * 1e-3) / 1e9
+        points_per_launch = args.steps * n_inst * L / max(nl, 1)
+        ach = bpp * points_per_launch / (launch_ms * 1e-3) / 1e9
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                 "frac": ach / peak, "traffic": None, "kernel": name, "bytes_per_point": bpp,
                 "launch_us": launch_ms * 1e3, "peak_source": peak_kind}
@@ -304,6 +309,13 @@ def run_ours(args):
                           launches if headline_split else launches2, 28.0, "k_gradient_split")
     roof_fp64 = roofline(t2_ms if headline_split else t_ms,
                          launches2 if headline_split else launches, 48.0, "k_gradient")
+    # DRAM bytes (read + write) per line point from one ncu capture of each
+    # kernel on a single 2^20-point line of this workload's kind, scaled to
+    # the points of one launch (traffic grows in proportion to the points).
+    pts_split = args.steps * n_inst * L / max(launches if headline_split else launches2, 1)
+    pts_fp64 = args.steps * n_inst * L / max(launches2 if headline_split else launches, 1)
+    roof_split["traffic"] = 35.224832e6 / L_FULL * pts_split
+    roof_fp64["traffic"] = 53.082624e6 / L_FULL * pts_fp64
 
     e2e = None
     cpu = None

@@ -209,6 +209,12 @@ qew_status qew_join_heights(qew_ctx *ctx, const qew_field *field,
 qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *field,
                               const int32_t *d_cell, const float *d_frac,
                               int n, const qew_params *p, float *d_grad);
+/* The same for `count` lines of n points on one field, stored contiguously
+ * (line k at offset k*n of each array), in one launch. */
+qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *field,
+                                    int count, const int32_t *d_cell,
+                                    const float *d_frac, int n,
+                                    const qew_params *p, float *d_grad);
 
 /* Line energy without device allocation. No counterpart in the reference:
  * an addition for callers that cannot call cudaMalloc where they need the

@@ -41,7 +41,8 @@ from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # n
 __all__ = [
     "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
     "SinusoidNoise", "AnalyticNoise", "objective", "objective_trial", "gradient",
-    "gradient_host", "split_heights", "join_heights", "gradient_split", "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "precond_apply",
+    "gradient_host", "split_heights", "join_heights", "gradient_split", "gradient_split_batch",
+    "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
     "depinning_bisect", "Context", "default_context", "QewError",
 ]
@@ -376,6 +377,28 @@ def gradient_split(cell, frac, p: Params, noise: "FilteredNoise", grad=None):
                                            C.byref(pc), C.c_void_p(grad.data_ptr())),
                 ctx.h, "gradient_split")
     return grad
+
+
+def gradient_split_batch(cells, fracs, p: Params, noise: "FilteredNoise", grads=None):
+    """gradient_split for a [count, n] batch of lines on one field, one launch."""
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    if cells.dim() != 2 or cells.shape != fracs.shape or not cells.is_contiguous() \
+            or not fracs.is_contiguous():
+        raise ValueError("expected contiguous [count, n] cells and fractions")
+    if cells.dtype != torch.int32 or fracs.dtype != torch.float32:
+        raise ValueError("expected int32 cells and float32 fractions")
+    count, n = cells.shape
+    if grads is None:
+        grads = torch.empty((count, n), dtype=torch.float32, device="cuda")
+    pc = p.c()
+    _capi.check(ctx.lib.qew_gradient_split_batch(ctx.h, noise.h, count,
+                                                 C.c_void_p(cells.data_ptr()),
+                                                 C.c_void_p(fracs.data_ptr()), n, C.byref(pc),
+                                                 C.c_void_p(grads.data_ptr())),
+                ctx.h, "gradient_split_batch")
+    return grads
 
 
 # ----------------------------------------------------------------- L-BFGS

@@ -88,6 +88,7 @@ _SIGS = {
     "qew_split_heights": (I, [VP, VP, VP, I, VP, VP]),
     "qew_join_heights": (I, [VP, VP, VP, VP, I, VP]),
     "qew_gradient_split": (I, [VP, VP, VP, VP, I, C.POINTER(qew_params), VP]),
+    "qew_gradient_split_batch": (I, [VP, VP, I, VP, VP, I, C.POINTER(qew_params), VP]),
     "qew_objective_noalloc": (I, [VP, VP, I, C.POINTER(qew_params), VP, VP]),
     "qew_lbfgs_default_params": (I, [C.POINTER(qew_lbfgs_params)]),
     "qew_lbfgs_minimize": (I, [VP, VP, VP, I, C.POINTER(qew_params),

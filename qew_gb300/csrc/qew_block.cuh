@@ -64,9 +64,9 @@ __device__ __forceinline__ void bsum3_all(double &a, double &b, double &c, doubl
 // gradient() of a whole line by one CTA (qew_model.h:149-193): edge pass into
 // ev/es, barrier, site combine into g. Ends with a barrier.
 template <class Noise, int BS>
-__device__ void block_gradient(const Noise &nz, const double *__restrict__ h, int n, double dx,
-                               double lt, double f, bool arc, double *ev, double *es,
-                               double *g) {
+__device__ void block_gradient(const Noise &nz, const double *__restrict__ h, int n,
+                               const LineDx &dx, double lt, double f, bool arc, double *ev,
+                               double *es, double *g) {
     for (int e = threadIdx.x; e < n; e += BS) {
         const int ep = (e + 1 == n) ? 0 : e + 1;
         double dv, sl;
@@ -86,8 +86,8 @@ __device__ void block_gradient(const Noise &nz, const double *__restrict__ h, in
 // objective() at x0 + alpha*d (alpha = 0: at x0) by one CTA.
 template <class Noise, int BS>
 __device__ double block_objective(const Noise &nz, const double *__restrict__ x0,
-                                  const double *__restrict__ d, double alpha, int n, double dx,
-                                  double lt, double f, int model, double *s_w) {
+                                  const double *__restrict__ d, double alpha, int n,
+                                  const LineDx &dx, double lt, double f, int model, double *s_w) {
     double acc = 0.0;
     for (int i = threadIdx.x; i < n; i += BS) {
         const int ip = (i + 1 == n) ? 0 : i + 1;

@@ -16,55 +16,67 @@
 
 namespace {
 
-// One periodic cubic B-spline prefilter along a line of N samples with
-// stride `st` (in elements) starting at p. Causal y[k] = s[k] + z y[k-1],
-// anticausal w[k] = y[k] + z w[k+1], c = -6 z w; the periodic sums for y[0]
-// and w[N-1] are Sum_j z^j (.)/(1 - z^N), truncated where z^j < 1e-37.
-__device__ void prefilter_line(double *p, long st, int N) {
-    const double z = -0.26794919243112270;  // sqrt(3) - 2
-    if (N == 1) return;                        // constant: c = s
-    const int K = N < 64 ? N : 64;
-    const double zN = pow(z, (double)N);
-    const double inv = 1.0 / (1.0 - zN);
-    double acc = 0, zk = 1;
-    for (int j = 0; j < K; ++j) {  // y[0] = Sum_j z^j s[(-j) mod N]
-        const int idx = (j == 0) ? 0 : N - j;
-        acc += zk * p[(long)idx * st];
-        zk *= z;
-    }
-    double prev = acc * inv;
-    p[0] = prev;
-    for (int k = 1; k < N; ++k) {
-        prev = p[(long)k * st] + z * prev;
-        p[(long)k * st] = prev;
-    }
-    acc = 0;
-    zk = 1;
-    for (int j = 0; j < K; ++j) {  // w[N-1] = Sum_j z^j y[(N-1+j) mod N]
-        const int idx = (j == 0) ? N - 1 : j - 1;
-        acc += zk * p[(long)idx * st];
-        zk *= z;
-    }
-    const double g = -6.0 * z;
-    double next = acc * inv;
-    p[(long)(N - 1) * st] = g * next;
-    for (int k = N - 2; k >= 0; --k) {
-        next = p[(long)k * st] + z * next;
-        p[(long)k * st] = g * next;
+// Periodic cubic B-spline prefilter along one axis, in two out-of-place
+// passes over chunks of kChunk samples so that every line is split over many
+// threads: causal y[k] = s[k] + z y[k-1], anticausal w[k] = y[k] + z w[k+1],
+// c = -6 z w. A chunk starts its recursion kWarm samples early (late, for the
+// anticausal pass) from zero, reading the periodic neighbours: the neglected
+// tail is z^kWarm ~ 5e-37 of the signal, so every output equals the exact
+// periodic solve up to rounding, for any N (the warm-up wraps for short N).
+// Lines are m = 0..M-1 at stride `lst`; samples at stride `st`; consecutive
+// threads take consecutive lines so each step's accesses coalesce when
+// lst == 1.
+constexpr double kPole = -0.26794919243112270;  // sqrt(3) - 2
+constexpr int kChunk = 256;
+constexpr int kWarm = 64;
+
+__device__ __forceinline__ int pmod(long k, int N) {
+    long r = k % N;
+    return (int)(r < 0 ? r + N : r);
+}
+
+__global__ void k_prefilter_causal(const double *__restrict__ in, double *__restrict__ out,
+                                   int N, long st, int M, long lst) {
+    const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int nchunks = (N + kChunk - 1) / kChunk;
+    if (tid >= (long)M * nchunks) return;
+    const int m = (int)(tid % M), c = (int)(tid / M);
+    const double *a = in + (long)m * lst;
+    double *b = out + (long)m * lst;
+    const int k0 = c * kChunk, k1 = min(k0 + kChunk, N);
+    double y = 0.0;
+    for (int k = k0 - kWarm; k < k0; ++k) y = a[(long)pmod(k, N) * st] + kPole * y;
+    for (int k = k0; k < k1; ++k) {
+        y = a[(long)k * st] + kPole * y;
+        b[(long)k * st] = y;
     }
 }
 
-// Host layout [nx][ny]: filter along x (stride ny) for every column j.
-// Consecutive threads take consecutive j, so each step's loads coalesce.
-__global__ void k_prefilter_x_hostlayout(double *a, int nx, int ny) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < ny) prefilter_line(a + j, ny, nx);
+__global__ void k_prefilter_anticausal(const double *__restrict__ in, double *__restrict__ out,
+                                       int N, long st, int M, long lst) {
+    const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int nchunks = (N + kChunk - 1) / kChunk;
+    if (tid >= (long)M * nchunks) return;
+    const int m = (int)(tid % M), c = (int)(tid / M);
+    const double *a = in + (long)m * lst;
+    double *b = out + (long)m * lst;
+    const int k0 = c * kChunk, k1 = min(k0 + kChunk, N);
+    const double gain = -6.0 * kPole;
+    double w = 0.0;
+    for (int k = k1 - 1 + kWarm; k >= k1; --k) w = a[(long)pmod(k, N) * st] + kPole * w;
+    for (int k = k1 - 1; k >= k0; --k) {
+        w = a[(long)k * st] + kPole * w;
+        b[(long)k * st] = gain * w;
+    }
 }
 
-// x-fastest [ny][nx]: filter along y (stride nx) for every column i.
-__global__ void k_prefilter_y_xfast(double *a, int nx, int ny) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < nx) prefilter_line(a + i, nx, ny);
+qew_status prefilter_axis(qew_ctx *ctx, double *a, double *work, int N, long st, int M,
+                          long lst) {
+    const long threads = (long)M * ((N + kChunk - 1) / kChunk);
+    const unsigned blocks = (unsigned)((threads + 255) / 256);
+    k_prefilter_causal<<<blocks, 256, 0, ctx->stream>>>(a, work, N, st, M, lst);
+    k_prefilter_anticausal<<<blocks, 256, 0, ctx->stream>>>(work, a, N, st, M, lst);
+    return qew_launch_check(ctx, "prefilter", 2);
 }
 
 // [nx][ny] -> [ny][nx] through a 32x33 shared tile.
@@ -140,10 +152,15 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
                                                   : cudaMemcpyHostToDevice,
                                     ctx->stream);
     if (e != cudaSuccess) return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "field upload: %s", cudaGetErrorString(e)));
-    k_prefilter_x_hostlayout<<<(ny + 127) / 128, 128, 0, ctx->stream>>>(tmp, nx, ny);
+    // x pass in the host layout (lines j, stride ny), transpose, y pass in
+    // the x-fastest layout (lines i, stride nx); c64 doubles as the work
+    // buffer of the first pass.
+    qew_status st = prefilter_axis(ctx, tmp, c64, nx, ny, ny, 1);
+    if (st != QEW_OK) return cleanup(st);
     k_transpose<<<dim3((ny + 31) / 32, (nx + 31) / 32), dim3(32, 8), 0, ctx->stream>>>(tmp, c64, nx, ny);
-    k_prefilter_y_xfast<<<(nx + 127) / 128, 128, 0, ctx->stream>>>(c64, nx, ny);
-    qew_status st = qew_launch_check(ctx, "prefilter", 3);
+    st = qew_launch_check(ctx, "transpose");
+    if (st != QEW_OK) return cleanup(st);
+    st = prefilter_axis(ctx, c64, tmp, ny, nx, nx, 1);
     if (st != QEW_OK) return cleanup(st);
     if (store & QEW_STORE_FP32) {
         if (cudaMalloc(&f->coef32, N * sizeof(float)) != cudaSuccess) {

@@ -15,6 +15,7 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <cstring>
 #include <string>
 
 #include "../../include/qew_gpu.h"
@@ -118,12 +119,50 @@ __device__ __forceinline__ void wrap4(int i, int n, int o[4]) {
     o[3] = (o[2] + 1 == n) ? 0 : o[2] + 1;
 }
 
+// True when d is a positive normal power of two: then x / d == x * (1/d)
+// exactly, so a division by d may be replaced by a multiplication.
+__host__ __device__ __forceinline__ bool dbl_is_pow2(double d) {
+#ifdef __CUDA_ARCH__
+    const long long b = __double_as_longlong(d);
+#else
+    long long b;
+    memcpy(&b, &d, sizeof(b));
+#endif
+    return d > 0 && (b & 0x000FFFFFFFFFFFFFLL) == 0 && ((b >> 52) & 0x7FF) != 0;
+}
+
+// Line spacing dx = physical_size / n with exact shortcuts for its divisions.
+struct LineDx {
+    double dx, inv_dx, inv_dx2;
+    bool pow2;
+    __host__ __device__ __forceinline__ double div(double v) const {
+        return pow2 ? v * inv_dx : v / dx;
+    }
+    __host__ __device__ __forceinline__ double div2(double v) const {  // v / (dx*dx)
+        return pow2 ? v * inv_dx2 : v / (dx * dx);
+    }
+};
+__host__ __device__ __forceinline__ LineDx make_line_dx(double physical_size, int n) {
+    LineDx L;
+    L.dx = physical_size / (double)n;
+    L.inv_dx = 1.0 / L.dx;
+    L.inv_dx2 = 1.0 / (L.dx * L.dx);
+    L.pow2 = dbl_is_pow2(L.dx);
+    return L;
+}
+
 // DeviceNoise on x-fastest FP64 coefficients.
 struct NoiseBSpline64 {
     const double *__restrict__ coef;  // [ny][nx]
     int nx, ny;
     double dx, dy, inv_dx, inv_dy;
     bool dx_pow2, dy_pow2;
+    // Set when the line has n == nx points over the field's length with a
+    // power-of-two spacing: every edge midpoint but the wrap edge is then at
+    // grid x = e + 1/2 exactly, so its cell is e and its x weights are those
+    // of t = 1/2 (bit-identical to locating it).
+    bool xconst;
+    double wxc[4];
 
     __device__ __forceinline__ double c(int ix, int iy) const {
         return __ldg(coef + (size_t)iy * (size_t)nx + ix);
@@ -170,6 +209,43 @@ struct NoiseBSpline64 {
             dg += wx[a] * row;
         }
         return dy_pow2 ? dg * inv_dy : dg / dy;
+    }
+    // dV/dy / V at the midpoint of edge e (xc its physical x).
+    __device__ __forceinline__ double dvdy_edge(int e, double xc, double y) const {
+        if (!xconst || e + 1 >= nx) return dvdy(xc, y);
+        int iy, xs[4], iyn[4];
+        double fy, dwy[4];
+        grid_locate(y, dy, inv_dy, dy_pow2, ny, iy, fy);
+        wrap4(e, nx, xs);
+        wrap4(iy, ny, iyn);
+        bsw_deriv(fy, dwy);
+        double dg = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) row += c(xs[a], iyn[b]) * dwy[b];
+            dg += wxc[a] * row;
+        }
+        return dy_pow2 ? dg * inv_dy : dg / dy;
+    }
+    __device__ __forceinline__ double value_edge(int e, double xc, double y) const {
+        if (!xconst || e + 1 >= nx) return value(xc, y);
+        int iy, xs[4], iyn[4];
+        double fy, wy[4];
+        grid_locate(y, dy, inv_dy, dy_pow2, ny, iy, fy);
+        wrap4(e, nx, xs);
+        wrap4(iy, ny, iyn);
+        bsw_value(fy, wy);
+        double v = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) row += c(xs[a], iyn[b]) * wy[b];
+            v += wxc[a] * row;
+        }
+        return v;
     }
     // sample, filtered_noise.h:103-134
     __device__ __forceinline__ void sample(double x, double y, double &v,
@@ -265,14 +341,41 @@ struct NoiseSinCos {  // AnalyticNoise{amp, kx, ky}
     }
 };
 
+// Edge accessors for every functor: the B-spline one has its own fast path.
+template <class Noise>
+__device__ __forceinline__ double noise_dvdy_edge(const Noise &nz, int, double xc, double y) {
+    return nz.dvdy(xc, y);
+}
+template <class Noise>
+__device__ __forceinline__ double noise_value_edge(const Noise &nz, int, double xc, double y) {
+    return nz.value(xc, y);
+}
+__device__ __forceinline__ double noise_dvdy_edge(const NoiseBSpline64 &nz, int e, double xc,
+                                                  double y) {
+    return nz.dvdy_edge(e, xc, y);
+}
+__device__ __forceinline__ double noise_value_edge(const NoiseBSpline64 &nz, int e, double xc,
+                                                   double y) {
+    return nz.value_edge(e, xc, y);
+}
+
 // Host helpers building the functors from a field handle.
 static inline bool qew_is_pow2(double d) {
     int e;
     const double m = frexp(d, &e);
     return d > 0 && m == 0.5;
 }
-static inline NoiseBSpline64 make_bspline64(const qew_field *f) {
+static inline NoiseBSpline64 make_bspline64(const qew_field *f, int n = 0,
+                                            double physical_size = 0) {
     NoiseBSpline64 nz;
+    nz.xconst = (n > 0 && n == f->nx && physical_size == f->Lx && qew_is_pow2(f->dx));
+    {
+        const double t = 0.5, s6 = 1.0 / 6.0, t2 = t * t, t3 = t2 * t, omt = 1.0 - t;
+        nz.wxc[0] = omt * omt * omt * s6;  // the host twin of bsw_value(0.5)
+        nz.wxc[1] = (4.0 - 6.0 * t2 + 3.0 * t3) * s6;
+        nz.wxc[2] = (1.0 + 3.0 * t + 3.0 * t2 - 3.0 * t3) * s6;
+        nz.wxc[3] = t3 * s6;
+    }
     nz.coef = f->coef64;
     nz.nx = f->nx;
     nz.ny = f->ny;
@@ -287,16 +390,17 @@ static inline NoiseBSpline64 make_bspline64(const qew_field *f) {
 
 // Calls `fn(noise_functor)` with the functor matching the field's kind.
 // Returns QEW_ERR_INVALID for an unknown kind or a B-spline field without
-// FP64 coefficients.
+// FP64 coefficients. n / physical_size describe the line (0: unknown).
 template <class Fn>
-qew_status qew_dispatch_noise(qew_ctx *ctx, const qew_field *f, Fn &&fn) {
+qew_status qew_dispatch_noise(qew_ctx *ctx, const qew_field *f, Fn &&fn, int n = 0,
+                              double physical_size = 0) {
     switch (f->kind) {
     case QEW_FIELD_BSPLINE:
         if (!f->coef64)
             return qew_fail(ctx, QEW_ERR_INVALID,
                             "field has no FP64 coefficients (created without "
                             "QEW_STORE_FP64)");
-        return fn(make_bspline64(f));
+        return fn(make_bspline64(f, n, physical_size));
     case QEW_FIELD_ZERO: return fn(NoiseZero{});
     case QEW_FIELD_CONST: return fn(NoiseConst{f->p0});
     case QEW_FIELD_HARMONIC: return fn(NoiseHarmonic{f->p0, f->p1});

@@ -82,7 +82,7 @@ qew_status qew_lbfgs_resident(qew_ctx *ctx, const qew_field *field, double *d_h,
         QEW_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         kern<<<1, kResBS, smem, ctx->stream>>>(nz, d_h, n, *p, cfg, pc, ws, npad, d_res);
         return qew_launch_check(ctx, "lbfgs_resident");
-    }));
+    }, n, p->physical_size));
     QEW_CUDA(ctx, cudaMemcpyAsync(res, d_res, sizeof(qew_lbfgs_result), cudaMemcpyDeviceToHost, ctx->stream));
     QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return QEW_OK;

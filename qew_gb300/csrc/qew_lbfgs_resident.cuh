@@ -57,7 +57,7 @@ __device__ void lbfgs_block(const Noise &nz, double *__restrict__ h, const int n
     __shared__ double s_b[BS];
     __shared__ LbfgsShared sh;
     const int t = threadIdx.x;
-    const double dx = P.physical_size / (double)n;
+    const LineDx dx = make_line_dx(P.physical_size, n);
     const double lt = P.line_tension, f = P.driving_force;
     const int model = P.model;
     const bool arc = (model == QEW_MODEL_ARCLENGTH);

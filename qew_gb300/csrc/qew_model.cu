@@ -27,14 +27,14 @@ qew_status objective_impl(qew_ctx *ctx, const qew_field *field, const At &at, in
                           const qew_params *p, double *h_out) {
     if (!ctx || !field || !p || !h_out || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "objective: bad arguments");
-    const double dx = p->physical_size / (double)n;
+    const LineDx dx = make_line_dx(p->physical_size, n);
     const int blocks = objective_blocks(n);
     QEW_TRY(qew_dispatch_noise(ctx, field, [&](auto nz) -> qew_status {
         k_objective<decltype(nz), At, kObjBS><<<blocks, kObjBS, 0, ctx->stream>>>(
             n, dx, p->line_tension, p->driving_force, p->model, nz, at, ctx->red_partials,
             ctx->red_counter, ctx->red_out);
         return qew_launch_check(ctx, "objective");
-    }));
+    }, n, p->physical_size));
     QEW_CUDA(ctx, cudaMemcpyAsync(ctx->host_out, ctx->red_out, sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));
     QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -48,7 +48,7 @@ qew_status qew_gradient_enqueue(qew_ctx *ctx, const qew_field *field, const doub
                                 const qew_params *p, int precision, double *d_grad) {
     if (!ctx || !field || !p || !d_h || !d_grad || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient: bad arguments");
-    const double dx = p->physical_size / (double)n;
+    const LineDx dx = make_line_dx(p->physical_size, n);
     const int blocks = (n + kGradBS - 1) / kGradBS;
     if (precision == QEW_PREC_FP32_SPLIT) {
         if (field->kind != QEW_FIELD_BSPLINE || !field->coef32)
@@ -62,7 +62,7 @@ qew_status qew_gradient_enqueue(qew_ctx *ctx, const qew_field *field, const doub
         k_gradient<decltype(nz), kGradBS><<<blocks, kGradBS, 0, ctx->stream>>>(
             d_h, n, dx, p->line_tension, p->driving_force, p->model, nz, d_grad);
         return qew_launch_check(ctx, "gradient");
-    });
+    }, n, p->physical_size);
 }
 
 extern "C" {

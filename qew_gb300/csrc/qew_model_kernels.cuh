@@ -19,55 +19,55 @@ struct TrialAt {  // x0 + alpha*d, never materialised (qew_model.h:92-98)
 // Energy of edge (i, ip): dx*(e_el + V(xc, hc) - f*h_i), qew_model.h:61-83.
 template <class Noise>
 __device__ __forceinline__ double edge_energy(const Noise &nz, int i, int ip, double hi,
-                                              double hip, double dx, double lt, double f,
+                                              double hip, const LineDx &L, double lt, double f,
                                               int model) {
-    const double dh_dx = (hip - hi) / dx;
+    const double dh_dx = L.div(hip - hi);
     double line_energy;
     if (model == QEW_MODEL_LINEAR)
         line_energy = lt * dh_dx * dh_dx * 0.5;
     else
         line_energy = lt * (sqrt(1.0 + dh_dx * dh_dx) - 1.0);
-    const double xc = (double)(i + ip) * 0.5 * dx;
+    const double xc = (double)(i + ip) * 0.5 * L.dx;
     const double hc = (hip + hi) * 0.5;
-    return dx * (line_energy + nz.value(xc, hc) - f * hi);
+    return L.dx * (line_energy + noise_value_edge(nz, i, xc, hc) - f * hi);
 }
 
 // Edge pass of gradient(), qew_model.h:163-175: dV/dy at the midpoint of edge
 // (e, e+1) and, for arclength, the normalised slope dh/sqrt(1+dh^2).
 template <class Noise>
 __device__ __forceinline__ void edge_gradient(const Noise &nz, int e, int n, double he,
-                                              double hep, double dx, bool arc, double &dv,
+                                              double hep, const LineDx &L, bool arc, double &dv,
                                               double &sl) {
     const int ep = (e + 1 == n) ? 0 : e + 1;
-    const double xc = (double)(e + ep) * 0.5 * dx;
+    const double xc = (double)(e + ep) * 0.5 * L.dx;
     const double hc = (hep + he) * 0.5;
-    dv = nz.dvdy(xc, hc);
+    dv = noise_dvdy_edge(nz, e, xc, hc);
     sl = 0.0;
     if (arc) {
-        const double dh = (hep - he) / dx;
+        const double dh = L.div(hep - he);
         sl = dh / sqrt(1.0 + dh * dh);
     }
 }
 
 // Per-site combine, qew_model.h:177-193.
 __device__ __forceinline__ double site_gradient(double hm, double h0, double hp, double dvl,
-                                                double dvr, double sll, double slr, double dx,
-                                                double lt, double f, bool arc) {
+                                                double dvr, double sll, double slr,
+                                                const LineDx &L, double lt, double f, bool arc) {
     double line_force;
     if (!arc) {
         const double d2h = hm + hp - 2.0 * h0;
-        line_force = -lt * d2h / (dx * dx);
+        line_force = L.div2(-lt * d2h);
     } else {
-        line_force = lt * (sll - slr) / dx;
+        line_force = L.div(lt * (sll - slr));
     }
-    return dx * (line_force + 0.5 * (dvl + dvr) - f);
+    return L.dx * (line_force + 0.5 * (dvl + dvr) - f);
 }
 
 // Fused gradient: CTA of BS sites stages h[base-1 .. base+BS] and the BS+1
 // edges it needs (its own plus the left halo edge) in shared memory.
 template <class Noise, int BS>
 __global__ void __launch_bounds__(BS)
-k_gradient(const double *__restrict__ h, int n, double dx, double lt, double f, int model,
+k_gradient(const double *__restrict__ h, int n, LineDx dx, double lt, double f, int model,
            Noise nz, double *__restrict__ grad) {
     __shared__ double s_h[BS + 2];
     __shared__ double s_dv[BS + 1];
@@ -94,7 +94,7 @@ k_gradient(const double *__restrict__ h, int n, double dx, double lt, double f, 
 // block to arrive (ticket counter, reset by that block for the next call).
 template <class Noise, class At, int BS>
 __global__ void __launch_bounds__(BS)
-k_objective(int n, double dx, double lt, double f, int model, Noise nz, At at,
+k_objective(int n, LineDx dx, double lt, double f, int model, Noise nz, At at,
             double *partials, unsigned int *counter, double *out) {
     __shared__ double s_w[BS / 32];
     __shared__ bool s_last;

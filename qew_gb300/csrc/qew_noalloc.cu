@@ -76,7 +76,7 @@ extern "C" qew_status qew_objective_noalloc(const qew_field *field, const double
         cudaGetLastError();
         return QEW_ERR_CUDA;
     }
-    const double dx = p->physical_size / (double)n;
+    const LineDx dx = make_line_dx(p->physical_size, n);
     const int blocks = (n + kNoAllocBS - 1) / kNoAllocBS;  // <= kNoAllocMaxBlocks
     return qew_dispatch_noise(nullptr, field, [&](auto nz) -> qew_status {
         k_objective<decltype(nz), LineAt, kNoAllocBS><<<blocks, kNoAllocBS, 0, stream>>>(
@@ -84,5 +84,5 @@ extern "C" qew_status qew_objective_noalloc(const qew_field *field, const double
             counter, d_out);
         const cudaError_t e = cudaGetLastError();
         return e == cudaSuccess ? QEW_OK : QEW_ERR_CUDA;
-    });
+    }, n, p->physical_size);
 }

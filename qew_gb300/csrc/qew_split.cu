@@ -104,35 +104,48 @@ __device__ __forceinline__ void split_mid(int c0, float f0, int c1, float f1, in
     }
 }
 
+// One CTA covers a tile of kTile = kBS * kItems consecutive sites of one line
+// (blockIdx.y selects the line of a batch stored contiguously, n apart).
+// Thread t owns sites t, t + kBS, ... of the tile, so every load phase is
+// coalesced, and each thread keeps 4 x 16 independent gathers in flight.
+constexpr int kItems = 4;
+constexpr int kTile = kBS * kItems;
+
 template <bool IN64, bool OUT64>
 __global__ void __launch_bounds__(kBS)
 k_gradient_split(const double *__restrict__ h64, const int *__restrict__ hc,
                  const float *__restrict__ hf, SplitGeom g, double *__restrict__ grad64,
                  float *__restrict__ grad32) {
-    __shared__ int s_c[kBS + 2];
-    __shared__ float s_f[kBS + 2];
-    __shared__ float s_dv[kBS + 1];
-    __shared__ float s_sl[kBS + 1];
+    __shared__ int s_c[kTile + 2];
+    __shared__ float s_f[kTile + 2];
+    __shared__ float s_dv[kTile + 1];
+    __shared__ float s_sl[kTile + 1];
     const int n = g.n;
-    const int base = blockIdx.x * kBS;
+    const size_t line = (size_t)blockIdx.y * (size_t)n;
+    if (IN64) h64 += line; else { hc += line; hf += line; }
+    if (OUT64) grad64 += line; else grad32 += line;
+    const int base = blockIdx.x * kTile;
     const int t = threadIdx.x;
-    const int i = base + t;
-    const int cnt = min(kBS, n - base);
+    const int cnt = min(kTile, n - base);
     auto load = [&](int site, int slot) {
         if (IN64) {
-            const double y = h64[site];
+            const double y = __ldcs(h64 + site);
             const double gy = g.dy_pow2 ? y * g.inv_dy : y / g.dy;
             const double fl = floor(gy);
             s_c[slot] = (int)fl;
             s_f[slot] = (float)(gy - fl);
         } else {
-            s_c[slot] = hc[site];
-            s_f[slot] = hf[site];
+            s_c[slot] = __ldcs(hc + site);
+            s_f[slot] = __ldcs(hf + site);
         }
     };
-    if (t < cnt) load(i, t + 1);
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int j = t + k * kBS;
+        if (j < cnt) load(base + j, j + 1);
+    }
     if (t == 0) load(base == 0 ? n - 1 : base - 1, 0);
-    if (t == cnt - 1) load((i + 1 == n) ? 0 : i + 1, cnt + 1);
+    if (t == kBS - 1) load((base + cnt == n) ? 0 : base + cnt, cnt + 1);
     __syncthreads();
     const bool arc = g.arc;
     auto edge = [&](int e, int sl, int sr, int out) {
@@ -146,23 +159,31 @@ k_gradient_split(const double *__restrict__ h64, const int *__restrict__ hc,
             s_sl[out] = dh * rsqrtf(1.0f + dh * dh);
         }
     };
-    if (t < cnt) edge(i, t + 1, t + 2, t + 1);
-    if (t == 0) edge(base == 0 ? n - 1 : base - 1, 0, 1, 0);
-    __syncthreads();
-    if (t >= cnt) return;
-    float line_force;
-    if (!arc) {
-        const float d2 = (float)(s_c[t] + s_c[t + 2] - 2 * s_c[t + 1]) +
-                         (s_f[t] + s_f[t + 2] - 2.0f * s_f[t + 1]);
-        line_force = -g.lt_dy_over_dx2 * d2;
-    } else {
-        line_force = g.lt_over_dx * (s_sl[t] - s_sl[t + 1]);
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int j = t + k * kBS;
+        if (j < cnt) edge(base + j, j + 1, j + 2, j + 1);
     }
-    const float gr = g.dx_f * (line_force + 0.5f * (s_dv[t] + s_dv[t + 1]) - g.f);
-    if (OUT64)
-        grad64[i] = (double)gr;
-    else
-        grad32[i] = gr;
+    if (t == kBS - 1) edge(base == 0 ? n - 1 : base - 1, 0, 1, 0);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+        const int j = t + k * kBS;
+        if (j >= cnt) break;
+        float line_force;
+        if (!arc) {
+            const float d2 = (float)(s_c[j] + s_c[j + 2] - 2 * s_c[j + 1]) +
+                             (s_f[j] + s_f[j + 2] - 2.0f * s_f[j + 1]);
+            line_force = -g.lt_dy_over_dx2 * d2;
+        } else {
+            line_force = g.lt_over_dx * (s_sl[j] - s_sl[j + 1]);
+        }
+        const float gr = g.dx_f * (line_force + 0.5f * (s_dv[j] + s_dv[j + 1]) - g.f);
+        if (OUT64)
+            __stcs(grad64 + base + j, (double)gr);
+        else
+            __stcs(grad32 + base + j, gr);
+    }
 }
 
 __global__ void k_split_heights(const double *__restrict__ h, int n, double dy, double inv_dy,
@@ -218,7 +239,7 @@ qew_status qew_gradient_split_enqueue(qew_ctx *ctx, const qew_field *f, const do
                                       const qew_params *p, double *d_grad) {
     QEW_TRY(split_check(ctx, f, n, p));
     const SplitGeom g = qew_split_geom(f, n, p);
-    k_gradient_split<true, true><<<(n + kBS - 1) / kBS, kBS, 0, ctx->stream>>>(
+    k_gradient_split<true, true><<<dim3((n + kTile - 1) / kTile, 1), kBS, 0, ctx->stream>>>(
         d_h, nullptr, nullptr, g, d_grad, nullptr);
     return qew_launch_check(ctx, "gradient_split64");
 }
@@ -248,9 +269,21 @@ qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *f, const int32_t *d
     if (!d_cell || !d_frac || !d_grad)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split: null buffer");
     const SplitGeom g = qew_split_geom(f, n, p);
-    k_gradient_split<false, false><<<(n + kBS - 1) / kBS, kBS, 0, ctx->stream>>>(
+    k_gradient_split<false, false><<<dim3((n + kTile - 1) / kTile, 1), kBS, 0, ctx->stream>>>(
         nullptr, d_cell, d_frac, g, nullptr, d_grad);
     return qew_launch_check(ctx, "gradient_split");
+}
+
+qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *f, int count,
+                                    const int32_t *d_cell, const float *d_frac, int n,
+                                    const qew_params *p, float *d_grad) {
+    QEW_TRY(split_check(ctx, f, n, p));
+    if (!d_cell || !d_frac || !d_grad || count < 1 || count > 65535)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split_batch: bad arguments");
+    const SplitGeom g = qew_split_geom(f, n, p);
+    k_gradient_split<false, false><<<dim3((n + kTile - 1) / kTile, count), kBS, 0, ctx->stream>>>(
+        nullptr, d_cell, d_frac, g, nullptr, d_grad);
+    return qew_launch_check(ctx, "gradient_split_batch");
 }
 
 }  // extern "C"

@@ -92,3 +92,21 @@ def test_split_needs_fp32_storage(Q):
     f = Q.FilteredNoise(band_limited_field(64, 32, 3.2, 1.0, 1.0, 0.3, 1), 3.2, 1.0)
     with pytest.raises(ValueError, match="FP32"):
         Q.gradient(t64(np.zeros(64)), Q.Params(3.2), f, precision=Q.QEW_PREC_FP32_SPLIT)
+
+
+def test_split_batch_equals_single_lines(Q):
+    import torch
+    n, ny, count = 5000, 48, 5
+    f = Q.FilteredNoise(gaussian_field(n, ny, 3.0, 8), float(n), float(ny),
+                        store=Q.QEW_STORE_FP32)
+    rng = np.random.default_rng(9)
+    hs = [t64(ny / 2 + np.cumsum(rng.standard_normal(n)) * 0.1) for _ in range(count)]
+    sp = [Q.split_heights(h, f) for h in hs]
+    cells = torch.stack([c for c, _ in sp]).contiguous()
+    fracs = torch.stack([fr for _, fr in sp]).contiguous()
+    for model in (Q.Model.Linear, Q.Model.Arclength):
+        p = Q.Params(float(n), 0.8, 0.05, model)
+        gb = npy(Q.gradient_split_batch(cells, fracs, p, f))
+        for k in range(count):
+            gk = npy(Q.gradient_split(sp[k][0], sp[k][1], p, f))
+            assert np.array_equal(gb[k], gk)
