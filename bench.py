@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--profile-run", action="store_true",
                     help="GPU timed loop only (no e2e, CPU baseline or clock sampling)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ensemble-lines", type=int, default=4096,
+                    help="lines of the batched-statics section (0 skips it)")
+    ap.add_argument("--ensemble-ref", type=int, default=16,
+                    help="lines timed with the plain one-line-per-launch form")
     return ap.parse_args()
 
 
@@ -213,6 +217,71 @@ def run_reference(args):
     return 0
 
 
+# ----------------------------------------------------------- ensemble (C3)
+def run_ensemble(args, Q, torch):
+    """Batched statics: `lines` realisations, L log-uniform in [256, 16384]
+    (even), each on its own 256-row field (Gaussian filter, xi ~ U[2, 8]
+    cells, unit variance, generated on the device), linear or arclength with
+    probability 1/2, Gamma = 1, f = 0, h0 = 0; L-BFGS m = 10, preconditioned
+    (shift 0.5/xi^2), FP32 split-gather phase to 2e-5 then FP64 refinement to
+    max|g| < 1e-8. Compared with the plain one-line-per-launch FP64 form
+    (same parameters) on a uniform random sample of the lines."""
+    rng = np.random.default_rng(3)
+    n_lines = args.ensemble_lines
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    specs, lines = [], []
+    for k in range(n_lines):
+        L = int(round(np.exp(rng.uniform(np.log(256), np.log(16384))) / 2)) * 2
+        xi = float(rng.uniform(2, 8))
+        model = Q.Model(int(rng.integers(0, 2)))
+        f = Q.FilteredNoise.generated(L, 256, float(L), 256.0, 1.0, xi, xi, 30000 + k, store=store)
+        p = Q.Params(float(L), 1.0, 0.0, model)
+        specs.append((L, xi, p, f))
+        lines.append((torch.zeros(L, dtype=torch.float64, device="cuda"), p, f, 0.5 / xi ** 2))
+    lp = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=20000, precondition=True, ls_fallback=True)
+    torch.cuda.synchronize()
+    ctx = Q.default_context()
+    l0 = ctx.launches()
+    t0 = time.perf_counter()
+    res = Q.ensemble_minimize(lines, lp, ftol_fp32=2e-5)
+    torch.cuda.synchronize()
+    t_ens = time.perf_counter() - t0
+    launches = ctx.launches() - l0
+    conv = sum(r.converged for r in res)
+    gmax = max(float(Q.gradient(h, p, f).abs().max()) for h, p, f, _ in lines)
+    iters = [r.iterations for r in res]
+    # plain comparator on a sample
+    sample = rng.choice(n_lines, size=min(args.ensemble_ref, n_lines), replace=False)
+    t_plain, conv_plain, gmax_plain = [], 0, 0.0
+    for k in sample:
+        L, xi, p, f = specs[k]
+        h = torch.zeros(L, dtype=torch.float64, device="cuda")
+        lpk = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=20000, precondition=True,
+                            precond_shift=0.5 / xi ** 2, ls_fallback=True)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        r = Q.lbfgs_minimize(h, p, f, lpk, form=Q.QEW_LBFGS_PLAIN)
+        torch.cuda.synchronize()
+        t_plain.append(time.perf_counter() - t1)
+        conv_plain += int(r.converged)
+        gmax_plain = max(gmax_plain, float(Q.gradient(h, p, f).abs().max()))
+    plain_rate = 1.0 / float(np.mean(t_plain))
+    rate = n_lines / t_ens
+    for h, p, f, _ in lines:
+        del h
+    return {"metric": "ensemble solves/s at max|grad| < 1e-8 (FP64-refined)", "value": rate,
+            "unit": "solves/s", "lines": n_lines, "wall_s": t_ens, "converged": conv,
+            "verified_max_grad": gmax, "iterations_median": float(np.median(iters)),
+            "gpu_launches": launches,
+            "workload": "L log-uniform [256,16384], 256-row fields, xi~U[2,8], h0=0, m=10, "
+                        "preconditioned, FP32 phase to 2e-5 then FP64 to 1e-8",
+            "plain_fp64_one_line_per_launch": {
+                "value": plain_rate, "unit": "solves/s", "sample_lines": int(len(sample)),
+                "converged": conv_plain, "verified_max_grad": gmax_plain,
+                "mean_s_per_solve": float(np.mean(t_plain))},
+            "speedup_vs_plain": rate / plain_rate}
+
+
 # ---------------------------------------------------------------- our arm
 def timed(torch, fn, steps, ctx):
     """Run fn() `steps` times between CUDA events on the current stream;
@@ -315,7 +384,7 @@ def run_ours(args):
     pts_split = args.steps * n_inst * L / max(launches if headline_split else launches2, 1)
     pts_fp64 = args.steps * n_inst * L / max(launches2 if headline_split else launches, 1)
     roof_split["traffic"] = 35.224832e6 / L_FULL * pts_split
-    roof_fp64["traffic"] = 53.082624e6 / L_FULL * pts_fp64
+    roof_fp64["traffic"] = 53.188352e6 / L_FULL * pts_fp64
 
     e2e = None
     cpu = None
@@ -335,6 +404,12 @@ def run_ours(args):
         e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
                "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
                "call": "qew_gradient_host (FP64 host heights in, FP64 host gradient out)"}
+    ensemble = None
+    if not args.profile_run and args.ensemble_lines > 0:
+        del noise, cells, fracs, g32, g64, hs
+        torch.cuda.empty_cache()
+        ensemble = run_ensemble(args, Q, torch)
+    if not args.profile_run:
         if rank == 0 and args.cpu_seconds > 0:
             cpu = cpu_gradient_rate(args.cpu_seconds)
 
@@ -355,7 +430,7 @@ def run_ours(args):
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "roofline": roof_split if headline_split else roof_fp64,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-                "other_precision": other}
+                "other_precision": other, "ensemble": ensemble}
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

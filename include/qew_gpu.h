@@ -81,7 +81,12 @@ enum { QEW_STORE_FP64 = 1, QEW_STORE_FP32 = 2 };
  * arithmetic); its error against FP64 is about 1e-6 of the gradient scale. */
 enum { QEW_PREC_FP64 = 0, QEW_PREC_FP32_SPLIT = 1 };
 
-/* LbfgsParams, lbfgs.h:32-52 (same fields, same defaults). */
+/* LbfgsParams, lbfgs.h:32-52 (same fields, same defaults), plus
+ * ls_fallback (no reference counterpart; default 0 = the reference's Armijo
+ * search alone): 1 adds the approximate-Wolfe slope test (Hager & Zhang,
+ * 2005) when the Armijo energy test fails, which lets the solve reach
+ * gradient tolerances near 1e-8 where energy differences are below the
+ * rounding of the energy. */
 typedef struct {
     int m;
     double ftol;
@@ -92,6 +97,7 @@ typedef struct {
     double curvature_eps;
     int precondition;
     double precond_shift;
+    int ls_fallback;
 } qew_lbfgs_params;
 
 /* LbfgsResult, lbfgs.h:54-61 */
@@ -156,6 +162,18 @@ qew_status qew_field_create_from_host(qew_ctx *ctx, const double *h_field,
 qew_status qew_field_create_from_device(qew_ctx *ctx, const double *d_field,
                                         int nx, int ny, double Lx, double Ly,
                                         int store_flags, qew_field **out);
+/* Synthetic field generated on the device (no reference counterpart; the
+ * on-device replacement of the host generation in FilteredNoise's seeded
+ * constructor, filtered_noise.cpp:25-82, for per-request fields): white noise
+ * from the Philox stream of `seed`, a periodic Gaussian filter of standard
+ * deviation xi_x_cells / xi_y_cells grid cells along each axis (the real-space
+ * form of exp(-(2 pi xi f)^2 / 2)), scaled to population std `amplitude`
+ * (mean left in, as filtered_noise.cpp:61-79), then prefiltered as above. */
+qew_status qew_field_create_generated(qew_ctx *ctx, int nx, int ny, double Lx,
+                                      double Ly, double amplitude,
+                                      double xi_x_cells, double xi_y_cells,
+                                      uint64_t seed, int store_flags,
+                                      qew_field **out);
 /* Analytic potentials (see the kind enum). */
 qew_status qew_field_create_analytic(qew_ctx *ctx, int kind, double p0,
                                      double p1, double p2, qew_field **out);
@@ -253,6 +271,33 @@ qew_status qew_lbfgs_minimize_form(qew_ctx *ctx, const qew_field *field,
 qew_status qew_precond_apply(qew_ctx *ctx, const double *d_q, int n,
                              double line_tension, double physical_size,
                              double shift, int form, double *d_out);
+
+/* --------------------------------------------------------------- ensemble */
+/* Batched statics (no reference counterpart: the reference relaxes one line
+ * per lbfgs_minimize call, lbfgs.h:94-96). One entry per independent line. */
+typedef struct {
+    const qew_field *field;  /* B-spline field: FP64 coefficients, and FP32
+                                ones when the FP32 phase is used */
+    double *d_h;             /* n heights on the device, relaxed in place */
+    int n;
+    qew_params p;
+    double precond_shift;    /* per-line preconditioner shift (<= 0: auto) */
+} qew_ensemble_line;
+
+typedef struct {
+    qew_lbfgs_params lbfgs;  /* m, final FP64 ftol, limits, line search */
+    double ftol_fp32;        /* > 0: first relax on the FP32 split gather to
+                                max|g| < ftol_fp32, then refine in FP64 */
+    int max_iter_fp32;       /* iteration cap of that phase (<= 0: max_iter) */
+} qew_ensemble_params;
+
+/* Relaxes every line; results[k] describes line k (iterations and
+ * evaluations of both phases summed, max_force/converged of the FP64
+ * refinement). One persistent launch, longest lines first. */
+qew_status qew_ensemble_minimize(qew_ctx *ctx, int count,
+                                 const qew_ensemble_line *lines,
+                                 const qew_ensemble_params *ep,
+                                 qew_lbfgs_result *results);
 
 /* --------------------------------------------------------------- Langevin */
 /* LangevinDynamics(n, seed), dynamics.h:31-32. Increments are N(0,1) from a

@@ -37,7 +37,7 @@ class QoParams(C.Structure):
 class QoLbfgsParams(C.Structure):
     _fields_ = [("m", I), ("ftol", D), ("max_iter", I), ("c1", D),
                 ("ls_shrink", D), ("max_ls", I), ("curvature_eps", D),
-                ("precondition", I), ("precond_shift", D)]
+                ("precondition", I), ("precond_shift", D), ("ls_fallback", I)]
 
 
 class QoLbfgsResult(C.Structure):

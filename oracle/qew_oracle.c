@@ -468,6 +468,7 @@ void qo_lbfgs_default_params(qo_lbfgs_params *lp) { /* lbfgs.h:32-52 */
     lp->curvature_eps = 1e-12;
     lp->precondition = 0;
     lp->precond_shift = 0;
+    lp->ls_fallback = 0;
 }
 
 static double qo_dot(int n, const double *a, const double *b) { /* lbfgs.h:65-71 */
@@ -617,7 +618,7 @@ int qo_lbfgs_minimize(double *h, int n, const qo_params *p,
             const double gn = sqrt(qo_dot(n, g, g));
             alpha = 1.0 / (gn > 1.0 ? gn : 1.0);
         }
-        int ok = 0;
+        int ok = 0, have_gn = 0;
         for (int ls = 0; ls < lp->max_ls; ++ls) {
             const double phi_trial = qo_objective_trial(h, d, alpha, n, p, nz);
             ++res->n_func_evals;
@@ -625,6 +626,21 @@ int qo_lbfgs_minimize(double *h, int n, const qo_params *p,
                 phi = phi_trial;
                 ok = 1;
                 break;
+            }
+            if (lp->ls_fallback) {
+                /* Extension, not in the reference: approximate-Wolfe test of
+                 * Hager & Zhang (2005) on the slope at q = h + alpha d. */
+                for (int i = 0; i < n; ++i) q[i] = h[i] + alpha * d[i];
+                qo_gradient(q, n, p, nz, g_new);
+                const double dphia = qo_dot(n, g_new, d);
+                ++res->n_func_evals;
+                if (dphia >= 0.9 * dphi0 && dphia <= (2.0 * 0.1 - 1.0) * dphi0 &&
+                    phi_trial <= phi0 + 1e-10 * fabs(phi0)) {
+                    phi = phi_trial;
+                    ok = 1;
+                    have_gn = 1;
+                    break;
+                }
             }
             alpha *= lp->ls_shrink;
         }
@@ -645,7 +661,7 @@ int qo_lbfgs_minimize(double *h, int n, const qo_params *p,
         const double al = alpha;
         for (int i = 0; i < n; ++i) h[i] += al * d[i];
         /* curvature pair, lbfgs.h:246-279 */
-        qo_gradient(h, n, p, nz, g_new);
+        if (!have_gn) qo_gradient(h, n, p, nz, g_new);
         double sy = 0, ss = 0, yy = 0;
         for (int i = 0; i < n; ++i) {
             const double s = al * d[i];

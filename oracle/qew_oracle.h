@@ -60,6 +60,8 @@ typedef struct { /* LbfgsParams, lbfgs.h:32-52 */
     double curvature_eps;
     int precondition;
     double precond_shift;
+    int ls_fallback; /* extension (not in the reference): approximate-Wolfe
+                        slope test when the Armijo test fails */
 } qo_lbfgs_params;
 
 typedef struct { /* LbfgsResult, lbfgs.h:54-61 */

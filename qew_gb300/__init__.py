@@ -42,7 +42,8 @@ __all__ = [
     "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
     "SinusoidNoise", "AnalyticNoise", "objective", "objective_trial", "gradient",
     "gradient_host", "split_heights", "join_heights", "gradient_split", "gradient_split_batch",
-    "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "precond_apply",
+    "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "ensemble_minimize",
+    "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
     "depinning_bisect", "Context", "default_context", "QewError",
 ]
@@ -81,12 +82,13 @@ class LbfgsParams:  # lbfgs.h:32-52
     curvature_eps: float = 1e-12
     precondition: bool = False
     precond_shift: float = 0.0
+    ls_fallback: bool = False  # extension: approximate-Wolfe fallback (see qew_gpu.h)
 
     def c(self) -> _capi.qew_lbfgs_params:
         return _capi.qew_lbfgs_params(int(self.m), float(self.ftol), int(self.max_iter),
                                       float(self.c1), float(self.ls_shrink), int(self.max_ls),
                                       float(self.curvature_eps), int(bool(self.precondition)),
-                                      float(self.precond_shift))
+                                      float(self.precond_shift), int(bool(self.ls_fallback)))
 
 
 @dataclass
@@ -229,6 +231,25 @@ class FilteredNoise(_Noise):
         self.nx, self.ny, self.Lx, self.Ly = nx, ny, float(Lx), float(Ly)
         self.dx, self.dy = self.Lx / nx, self.Ly / ny
         self.store = store
+
+    @classmethod
+    def generated(cls, nx: int, ny: int, Lx: float, Ly: float, amplitude: float,
+                  xi_x_cells: float, xi_y_cells: float, seed: int,
+                  store: int = QEW_STORE_FP64, ctx: Context | None = None) -> "FilteredNoise":
+        """A synthetic Gaussian-filtered field generated on the device."""
+        self = cls.__new__(cls)
+        _Noise.__init__(self)
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        _capi.check(self.ctx.lib.qew_field_create_generated(
+            self.ctx.h, int(nx), int(ny), float(Lx), float(Ly), float(amplitude),
+            float(xi_x_cells), float(xi_y_cells), int(seed), int(store), C.byref(h)),
+            self.ctx.h, "FilteredNoise.generated")
+        self.h = h
+        self.nx, self.ny, self.Lx, self.Ly = int(nx), int(ny), float(Lx), float(Ly)
+        self.dx, self.dy = self.Lx / nx, self.Ly / ny
+        self.store = store
+        return self
 
     def coefficients(self) -> np.ndarray:
         """The FP64 B-spline coefficients in the host layout [nx][ny]."""
@@ -414,6 +435,32 @@ def lbfgs_minimize(h, p: Params, noise: _Noise, lp: LbfgsParams | None = None,
                 ctx.h, "lbfgs_minimize")
     return LbfgsResult(res.iterations, res.max_force, bool(res.converged), res.n_func_evals,
                        res.n_curvature_skips, res.n_ls_restarts)
+
+
+def ensemble_minimize(lines, lp: LbfgsParams, ftol_fp32: float = 0.0, max_iter_fp32: int = 0,
+                      ctx: Context | None = None) -> list[LbfgsResult]:
+    """Relax many independent lines in one persistent launch.
+
+    ``lines`` is a list of (h, params, noise, precond_shift) with h a CUDA
+    float64 tensor relaxed in place. With ftol_fp32 > 0 each line is first
+    relaxed on the FP32 split gather, then refined in FP64 to lp.ftol.
+    """
+    ctx = ctx or default_context()
+    ctx.sync_stream()
+    n = len(lines)
+    arr = (_capi.qew_ensemble_line * max(n, 1))()
+    for k, (h, p, noise, shift) in enumerate(lines):
+        arr[k].field = noise.h
+        arr[k].d_h = _ptr(h)
+        arr[k].n = h.numel()
+        arr[k].p = p.c()
+        arr[k].precond_shift = float(shift)
+    ep = _capi.qew_ensemble_params(lp.c(), float(ftol_fp32), int(max_iter_fp32))
+    res = (_capi.qew_lbfgs_result * max(n, 1))()
+    _capi.check(ctx.lib.qew_ensemble_minimize(ctx.h, n, arr, C.byref(ep), res), ctx.h,
+                "ensemble_minimize")
+    return [LbfgsResult(r.iterations, r.max_force, bool(r.converged), r.n_func_evals,
+                        r.n_curvature_skips, r.n_ls_restarts) for r in res[:n]]
 
 
 def precond_apply(q, line_tension: float, physical_size: float, shift: float,

@@ -38,7 +38,8 @@ class qew_params(C.Structure):
 
 class qew_lbfgs_params(C.Structure):
     _fields_ = [("m", I), ("ftol", D), ("max_iter", I), ("c1", D), ("ls_shrink", D),
-                ("max_ls", I), ("curvature_eps", D), ("precondition", I), ("precond_shift", D)]
+                ("max_ls", I), ("curvature_eps", D), ("precondition", I), ("precond_shift", D),
+                ("ls_fallback", I)]
 
 
 class qew_lbfgs_result(C.Structure):
@@ -55,6 +56,14 @@ class qew_rk_params(C.Structure):
 class qew_rk_result(C.Structure):
     _fields_ = [("blocked", I), ("runaway", I), ("sweeps", I), ("total_advance", D),
                 ("mean_h", D)]
+
+
+class qew_ensemble_line(C.Structure):
+    _fields_ = [("field", VP), ("d_h", VP), ("n", I), ("p", qew_params), ("precond_shift", D)]
+
+
+class qew_ensemble_params(C.Structure):
+    _fields_ = [("lbfgs", qew_lbfgs_params), ("ftol_fp32", D), ("max_iter_fp32", I)]
 
 
 class QewError(RuntimeError):
@@ -77,6 +86,7 @@ _SIGS = {
     "qew_field_create_from_host": (I, [VP, PD, I, I, D, D, I, C.POINTER(VP)]),
     "qew_field_create_from_device": (I, [VP, VP, I, I, D, D, I, C.POINTER(VP)]),
     "qew_field_create_analytic": (I, [VP, I, D, D, D, C.POINTER(VP)]),
+    "qew_field_create_generated": (I, [VP, I, I, D, D, D, D, D, U64, I, C.POINTER(VP)]),
     "qew_field_destroy": (I, [VP]),
     "qew_field_get_coefficients": (I, [VP, VP, PD]),
     "qew_field_sample": (I, [VP, VP, VP, VP, I, VP, VP, VP]),
@@ -97,6 +107,8 @@ _SIGS = {
                                     C.POINTER(qew_lbfgs_params), I,
                                     C.POINTER(qew_lbfgs_result)]),
     "qew_precond_apply": (I, [VP, VP, I, D, D, D, I, VP]),
+    "qew_ensemble_minimize": (I, [VP, I, C.POINTER(qew_ensemble_line),
+                                  C.POINTER(qew_ensemble_params), C.POINTER(qew_lbfgs_result)]),
     "qew_langevin_create": (I, [VP, I, U64, C.POINTER(VP)]),
     "qew_langevin_destroy": (I, [VP]),
     "qew_langevin_step": (I, [VP, VP, VP, C.POINTER(qew_params), D, D]),

@@ -10,9 +10,11 @@
 // periodic initial conditions written in closed form, so the result equals
 // the FFT division up to rounding, for any nx, ny, in O(nx*ny) work.
 #include "qew_internal.cuh"
+#include "qew_philox.cuh"
 
 #include <cmath>
 #include <new>
+#include <vector>
 
 namespace {
 
@@ -113,6 +115,80 @@ __global__ void k_sample(Noise nz, const double *__restrict__ x, const double *_
     if (dvdy) dvdy[k] = c;
 }
 
+// ---- synthetic field generation on the device ----
+// White noise w[i][j] ~ N(0,1) from the Philox stream (seed, counter (pair of
+// j, row i)), then a periodic Gaussian filter of std xi cells along each axis
+// (the real-space form of exp(-(2 pi xi f)^2 / 2) in Fourier space; taps to
+// |k| <= ceil(5 xi), normalised so the sum of squared taps is 1), in the
+// reference's host layout [nx][ny].
+__global__ void k_white_noise(double *w, int nx, int ny, uint64_t seed) {
+    const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const int pairs = (ny + 1) / 2;
+    if (tid >= (long)nx * pairs) return;
+    const int i = (int)(tid / pairs), jp = (int)(tid % pairs);
+    double z0, z1;
+    philox_normal_pair(seed, (uint64_t)i, (uint32_t)jp, z0, z1);
+    w[(size_t)i * ny + 2 * jp] = z0;
+    if (2 * jp + 1 < ny) w[(size_t)i * ny + 2 * jp + 1] = z1;
+}
+
+// out[i][j] = sum_k taps[k] * in[(i + k - R) mod nx][j]   (axis 0), or along j (axis 1).
+__global__ void k_gauss_conv(const double *__restrict__ in, double *__restrict__ out, int nx,
+                             int ny, const double *__restrict__ taps, int R, int axis) {
+    const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (tid >= (long)nx * ny) return;
+    const int i = (int)(tid / ny), j = (int)(tid % ny);
+    double acc = 0.0;
+    for (int k = -R; k <= R; ++k) {
+        const double t = taps[k + R];
+        if (axis == 0)
+            acc += t * in[(size_t)pmod((long)i + k, nx) * ny + j];
+        else
+            acc += t * in[(size_t)i * ny + pmod((long)j + k, ny)];
+    }
+    out[tid] = acc;
+}
+
+__global__ void k_scale_inplace(double *a, size_t n, const double *scale) {
+    const double s = *scale;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x)
+        a[k] *= s;
+}
+
+// Population mean and std of n values -> scale = amplitude / std (one CTA).
+__global__ void k_std_scale(const double *__restrict__ a, size_t n, double amplitude,
+                            double *scale) {
+    __shared__ double s_w[32];
+    double s1 = 0.0;
+    for (size_t k = threadIdx.x; k < n; k += blockDim.x) s1 += a[k];
+    s1 = block_sum<1024>(s1, s_w);
+    __shared__ double s_mean;
+    if (threadIdx.x == 0) s_mean = s1 / (double)n;
+    __syncthreads();
+    const double mean = s_mean;
+    double s2 = 0.0;
+    for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
+        const double d = a[k] - mean;
+        s2 += d * d;
+    }
+    s2 = block_sum<1024>(s2, s_w);
+    if (threadIdx.x == 0) *scale = amplitude / sqrt(s2 / (double)n);
+}
+
+std::vector<double> gauss_taps(double xi, int &R) {
+    R = (xi > 0) ? (int)ceil(5.0 * xi) : 0;
+    std::vector<double> t(2 * R + 1);
+    double s2 = 0.0;
+    for (int k = -R; k <= R; ++k) {
+        const double v = (xi > 0) ? exp(-0.5 * (double)k * k / (xi * xi)) : 1.0;
+        t[k + R] = v;
+        s2 += v * v;
+    }
+    for (double &v : t) v /= sqrt(s2);
+    return t;
+}
+
 qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int nx,
                        int ny, double Lx, double Ly, int store, qew_field **out) {
     if (!ctx || !out || !src || nx <= 0 || ny <= 0 || !(Lx > 0) || !(Ly > 0) ||
@@ -199,6 +275,49 @@ qew_status qew_field_create_from_host(qew_ctx *ctx, const double *h_field, int n
 qew_status qew_field_create_from_device(qew_ctx *ctx, const double *d_field, int nx, int ny,
                                         double Lx, double Ly, int store_flags, qew_field **out) {
     return field_build(ctx, d_field, true, nx, ny, Lx, Ly, store_flags, out);
+}
+
+qew_status qew_field_create_generated(qew_ctx *ctx, int nx, int ny, double Lx, double Ly,
+                                     double amplitude, double xi_x_cells, double xi_y_cells,
+                                     uint64_t seed, int store_flags, qew_field **out) {
+    if (!ctx || !out || nx <= 0 || ny <= 0 || !(xi_x_cells >= 0) || !(xi_y_cells >= 0) ||
+        xi_x_cells > 4096 || xi_y_cells > 4096 || !(amplitude > 0))
+        return qew_fail(ctx, QEW_ERR_INVALID, "field_create_generated: bad arguments");
+    QEW_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t N = (size_t)nx * ny;
+    int Rx, Ry;
+    const std::vector<double> tx = gauss_taps(xi_x_cells, Rx), ty = gauss_taps(xi_y_cells, Ry);
+    double *w = nullptr, *t = nullptr, *taps = nullptr;
+    auto cleanup = [&](qew_status s) {
+        if (w) cudaFree(w);
+        if (t) cudaFree(t);
+        if (taps) cudaFree(taps);
+        return s;
+    };
+    if (cudaMalloc(&w, N * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&t, N * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&taps, (tx.size() + ty.size() + 1) * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return cleanup(qew_fail(ctx, QEW_ERR_NOMEM, "field_create_generated: cudaMalloc"));
+    }
+    double *tapx = taps, *tapy = taps + tx.size(), *scale = tapy + ty.size();
+    cudaError_t e = cudaMemcpyAsync(tapx, tx.data(), tx.size() * sizeof(double),
+                                    cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(tapy, ty.data(), ty.size() * sizeof(double), cudaMemcpyHostToDevice,
+                            ctx->stream);
+    if (e != cudaSuccess) return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "%s", cudaGetErrorString(e)));
+    const long pairs = (long)nx * ((ny + 1) / 2);
+    k_white_noise<<<(unsigned)((pairs + 255) / 256), 256, 0, ctx->stream>>>(w, nx, ny, seed);
+    const unsigned blocks = (unsigned)((N + 255) / 256);
+    k_gauss_conv<<<blocks, 256, 0, ctx->stream>>>(w, t, nx, ny, tapy, Ry, 1);
+    k_gauss_conv<<<blocks, 256, 0, ctx->stream>>>(t, w, nx, ny, tapx, Rx, 0);
+    k_std_scale<<<1, 1024, 0, ctx->stream>>>(w, N, amplitude, scale);
+    k_scale_inplace<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(w, N, scale);
+    qew_status st = qew_launch_check(ctx, "field_generate", 5);
+    if (st != QEW_OK) return cleanup(st);
+    st = field_build(ctx, w, true, nx, ny, Lx, Ly, store_flags, out);
+    return cleanup(st);
 }
 
 qew_status qew_field_create_analytic(qew_ctx *ctx, int kind, double p0, double p1, double p2,

@@ -198,7 +198,7 @@ qew_status qew_lbfgs_plain(qew_ctx *ctx, const qew_field *field, double *d_h, in
             QEW_TRY(dot(g, g, gg));
             alpha = 1.0 / std::max(1.0, std::sqrt(gg));
         }
-        bool ok = false;
+        bool ok = false, have_gn = false;
         for (int ls = 0; ls < lp->max_ls; ++ls) {
             double phi_trial;
             QEW_TRY(qew_objective_trial(ctx, field, d_h, d, alpha, n, p, &phi_trial));
@@ -207,6 +207,22 @@ qew_status qew_lbfgs_plain(qew_ctx *ctx, const qew_field *field, double *d_h, in
                 phi = phi_trial;
                 ok = true;
                 break;
+            }
+            if (lp->ls_fallback) {  // approximate-Wolfe slope test at q = h + alpha d
+                QEW_CUDA(ctx, cudaMemcpyAsync(q, d_h, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                              ctx->stream));
+                QEW_TRY(axpy(alpha, d, q));
+                QEW_TRY(qew_gradient_enqueue(ctx, field, q, n, p, QEW_PREC_FP64, g_new));
+                double dphia;
+                QEW_TRY(dot(g_new, d, dphia));
+                ++res->n_func_evals;
+                if (dphia >= 0.9 * dphi0 && dphia <= (2.0 * 0.1 - 1.0) * dphi0 &&
+                    phi_trial <= phi0 + 1e-10 * std::fabs(phi0)) {
+                    phi = phi_trial;
+                    ok = true;
+                    have_gn = true;
+                    break;
+                }
             }
             alpha *= lp->ls_shrink;
         }
@@ -223,7 +239,7 @@ qew_status qew_lbfgs_plain(qew_ctx *ctx, const qew_field *field, double *d_h, in
         }
         ls_fail_streak = 0;
         QEW_TRY(axpy(alpha, d, d_h));  // lbfgs_step, lbfgs.h:243-244
-        QEW_TRY(qew_gradient_enqueue(ctx, field, d_h, n, p, QEW_PREC_FP64, g_new));
+        if (!have_gn) QEW_TRY(qew_gradient_enqueue(ctx, field, d_h, n, p, QEW_PREC_FP64, g_new));
         double syy[3];
         QEW_TRY((vec_reduce<SyF, 3, false>(ctx, n, SyF{d, g_new, g, s_tmp, y_tmp, alpha}, syy)));
         const double sy = syy[0], ss = syy[1], yy = syy[2];
@@ -286,6 +302,7 @@ qew_status qew_lbfgs_default_params(qew_lbfgs_params *lp) {
     lp->curvature_eps = 1e-12;
     lp->precondition = 0;
     lp->precond_shift = 0;
+    lp->ls_fallback = 0;
     return QEW_OK;
 }
 

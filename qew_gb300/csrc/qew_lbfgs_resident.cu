@@ -51,7 +51,8 @@ __global__ void __launch_bounds__(BS)
 k_lbfgs_single(Noise nz, double *h, int n, qew_params P, LbfgsCfg cfg, PrecondCoef pc,
                double *ws, size_t npad, qew_lbfgs_result *out) {
     extern __shared__ double s_dyn[];
-    lbfgs_block<Noise, BS>(nz, h, n, P, cfg, pc, ws, npad, out, s_dyn);
+    const qew_lbfgs_result r = lbfgs_block<Noise, BS>(nz, h, n, P, cfg, pc, ws, npad);
+    if (threadIdx.x == 0) *out = r;
 }
 
 }  // namespace

@@ -17,7 +17,17 @@ struct LbfgsCfg {
     int max_ls;
     double curvature_eps;
     int precondition;
+    int ls_fallback;
 };
+
+// Approximate-Wolfe test (W. Hager, H. Zhang, SIAM J. Optim. 16 (2005)),
+// tried when the Armijo energy test fails: sigma*phi'(0) <= phi'(a) <=
+// (2*delta - 1)*phi'(0) and phi(a) <= phi(0) + eps*|phi(0)|. It decides on
+// slopes, which keep their relative accuracy where energy differences drown
+// in the rounding of |E| (the regime of a ~1e-8 gradient tolerance).
+constexpr double kAwDelta = 0.1;
+constexpr double kAwSigma = 0.9;
+constexpr double kAwEps = 1e-10;
 
 inline LbfgsCfg lbfgs_cfg_from(const qew_lbfgs_params *lp) {
     LbfgsCfg c;
@@ -29,6 +39,7 @@ inline LbfgsCfg lbfgs_cfg_from(const qew_lbfgs_params *lp) {
     c.max_ls = lp->max_ls;
     c.curvature_eps = lp->curvature_eps;
     c.precondition = lp->precondition;
+    c.ls_fallback = lp->ls_fallback;
     return c;
 }
 
@@ -50,9 +61,9 @@ struct LbfgsShared {
 // Workspace (npad-strided vectors): g, g_new, d, q, ev, es, then 2(m+1)
 // history buffers (m S rows + spare, m Y rows + spare).
 template <class Noise, int BS>
-__device__ void lbfgs_block(const Noise &nz, double *__restrict__ h, const int n,
+__device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h, const int n,
                             const qew_params P, const LbfgsCfg cfg, const PrecondCoef pc,
-                            double *ws, size_t npad, qew_lbfgs_result *out, double * /*dyn*/) {
+                            double *ws, size_t npad) {
     __shared__ double s_w[96];
     __shared__ double s_b[BS];
     __shared__ LbfgsShared sh;
@@ -165,7 +176,7 @@ __device__ void lbfgs_block(const Noise &nz, double *__restrict__ h, const int n
             for (int i = t; i < n; i += BS) gg += g[i] * g[i];
             alpha = 1.0 / fmax(1.0, sqrt(bsum_all<BS>(gg, s_w)));
         }
-        bool ok = false;
+        bool ok = false, have_gn = false;
         for (int ls = 0; ls < cfg.max_ls; ++ls) {
             const double pt = block_objective<Noise, BS>(nz, h, d, alpha, n, dx, lt, f, model, s_w);
             ++res.n_func_evals;
@@ -173,6 +184,22 @@ __device__ void lbfgs_block(const Noise &nz, double *__restrict__ h, const int n
                 phi = pt;
                 ok = true;
                 break;
+            }
+            if (cfg.ls_fallback) {  // slope test at the trial point, q = h + alpha d
+                for (int i = t; i < n; i += BS) q[i] = h[i] + alpha * d[i];
+                __syncthreads();
+                block_gradient<Noise, BS>(nz, q, n, dx, lt, f, arc, ev, es, gn);
+                double sd = 0.0;
+                for (int i = t; i < n; i += BS) sd += gn[i] * d[i];
+                const double dphia = bsum_all<BS>(sd, s_w);
+                ++res.n_func_evals;
+                if (dphia >= kAwSigma * dphi0 && dphia <= (2.0 * kAwDelta - 1.0) * dphi0 &&
+                    pt <= phi0 + kAwEps * fabs(phi0)) {
+                    phi = pt;
+                    ok = true;
+                    have_gn = true;  // gn already holds the gradient at the new point
+                    break;
+                }
             }
             alpha *= cfg.ls_shrink;
         }
@@ -192,7 +219,7 @@ __device__ void lbfgs_block(const Noise &nz, double *__restrict__ h, const int n
         ls_fail_streak = 0;
         for (int i = t; i < n; i += BS) h[i] += alpha * d[i];  // lbfgs.h:243-244
         __syncthreads();
-        block_gradient<Noise, BS>(nz, h, n, dx, lt, f, arc, ev, es, gn);
+        if (!have_gn) block_gradient<Noise, BS>(nz, h, n, dx, lt, f, arc, ev, es, gn);
         double *sT = bufs + (size_t)sh.stmp * npad;
         double *yT = bufs + (size_t)sh.ytmp * npad;
         double sy = 0.0, ss = 0.0, yy = 0.0;
@@ -241,7 +268,7 @@ __device__ void lbfgs_block(const Noise &nz, double *__restrict__ h, const int n
         res.max_force = bmax_all<BS>(lm, s_w);
         res.converged = 0;
     }
-    if (t == 0) *out = res;
+    return res;  // identical in every thread
 }
 
 size_t qew_lbfgs_resident_ws_doubles(int n, int m);
