@@ -56,6 +56,14 @@ def parse():
                     help="lines of the batched-statics section (0 skips it)")
     ap.add_argument("--ensemble-ref", type=int, default=16,
                     help="lines timed with the plain one-line-per-launch form")
+    ap.add_argument("--sections", default="ensemble,dynamics,depinning",
+                    help="extra configurations reported beside the headline")
+    ap.add_argument("--dyn-steps", type=int, default=100000)
+    ap.add_argument("--dyn-plain-steps", type=int, default=2000)
+    ap.add_argument("--dep-size", type=int, default=16384)
+    ap.add_argument("--dep-fstep", type=float, default=0.05)
+    ap.add_argument("--dep-fmax", type=float, default=20.0)
+    ap.add_argument("--dep-rate-sweeps", type=int, default=2000)
     return ap.parse_args()
 
 
@@ -282,6 +290,116 @@ def run_ensemble(args, Q, torch):
             "speedup_vs_plain": rate / plain_rate}
 
 
+# ------------------------------------------------------------ dynamics (C1)
+def run_dynamics(args, Q, torch):
+    """Annealed overdamped Langevin: L = 65536, 65536 x 4096 field (xi = 4
+    cells, seed 1), arclength, f = 0.5, Gamma = 1, T from 0.5 to 0 linearly
+    over the steps, dt = 0.01 (drift = dt, diff = sqrt(2 T dt)), Philox
+    increments of seed 1; FP64 and FP32-gather runs in one device-resident
+    launch each, and the plain per-step form (gradient + update launches) on
+    the first steps."""
+    n, ny, K = 65536, 4096, args.dyn_steps
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    f = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 1, store=store)
+    p = Q.Params(float(n), 1.0, 0.5, Q.Model.Arclength)
+    dt = 0.01
+    T = 0.5 * (1.0 - np.arange(K) / K)
+    drift = np.full(K, dt)
+    diff = np.sqrt(2.0 * T * dt)
+    out = {"metric": "Langevin steps/s (L=65536)", "unit": "steps/s", "steps": K,
+           "workload": "L=65536, 65536x4096 field xi=4, arclength, f=0.5, T 0.5->0, dt=0.01"}
+    for name, prec in (("fp64", Q.QEW_PREC_FP64), ("fp32split", Q.QEW_PREC_FP32_SPLIT)):
+        h = torch.full((n,), 0.5 * ny, dtype=torch.float64, device="cuda")
+        dyn = Q.LangevinDynamics(n, 1)
+        dyn.run(h, p, f, drift[:10], diff[:10], precision=prec)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dyn.run(h, p, f, drift, diff, precision=prec)
+        torch.cuda.synchronize()
+        dt_s = time.perf_counter() - t0
+        out[name] = {"value": K / dt_s, "points_per_s": K * n / dt_s, "wall_s": dt_s,
+                     "final_mean_h": float(h.mean()), "final_std_h": float(h.std())}
+    Kp = min(K, args.dyn_plain_steps)
+    h = torch.full((n,), 0.5 * ny, dtype=torch.float64, device="cuda")
+    dyn = Q.LangevinDynamics(n, 1)
+    dyn.step(h, p, f, drift[0], diff[0])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(Kp):
+        dyn.step(h, p, f, drift[k], diff[k])
+    torch.cuda.synchronize()
+    out["plain_fp64_per_step_launches"] = {"value": Kp / (time.perf_counter() - t0),
+                                           "steps": Kp}
+    out["value"] = out["fp64"]["value"]
+    return out
+
+
+# ----------------------------------------------------------- depinning (C2)
+def run_depinning(args, Q, torch):
+    """Rosso-Krauth depinning: L = 16384, 16384^2 field (xi = 4 cells, seed 2,
+    unit variance), linear, Gamma = 1, flat start at Ly/2; dstep = 0.5 cell,
+    max_advance = Ly, runaway = 2 Ly, root_tol 1e-10, sweep_tol 1e-8. Ramp f
+    by f_step until a block fails, then bisect f to 1e-10 relative from the
+    last blocked line. FP64 and FP32-velocity forms; the plain host-driven
+    form is timed on one block for its sweep rate."""
+    n = ny = args.dep_size
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    fld = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2, store=store)
+    rp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
+                    runaway=2.0 * ny, max_sweeps=200000)
+    out = {"metric": "time to f_c (ramp + bisection to 1e-10)", "unit": "s",
+           "workload": "L=%d, %dx%d field xi=4, linear, Gamma=1, f_step=%g" % (n, n, ny, args.dep_fstep)}
+    crit = {}
+    for name, prec in (("fp64", Q.QEW_PREC_FP64), ("fp32split", Q.QEW_PREC_FP32_SPLIT)):
+        h = torch.full((n,), 0.5 * ny, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sweeps, blocks, f_lo, f_hi, h_lo = 0, 0, None, None, None
+        k = 0
+        while k * args.dep_fstep <= args.dep_fmax:
+            fk = k * args.dep_fstep
+            r = Q.rk_block(h, Q.Params(float(n), 1.0, fk, Q.Model.Linear), fld, rp, precision=prec)
+            sweeps += r.sweeps
+            blocks += 1
+            if not r.blocked:
+                f_hi = fk
+                break
+            f_lo, h_lo = fk, h.clone()
+            k += 1
+        res = {"ramp_blocks": blocks, "ramp_sweeps": sweeps, "f_lo": f_lo, "f_hi": f_hi}
+        if f_lo is not None and f_hi is not None:
+            fc, flo, fhi, nb = Q.depinning_bisect(h_lo, Q.Params(float(n), 1.0, 0.0, Q.Model.Linear),
+                                                  fld, rp, f_lo, f_hi, rtol=1e-10, max_steps=64,
+                                                  precision=prec)
+            torch.cuda.synchronize()
+            res.update({"f_c": fc, "bracket": [flo, fhi], "bisect_blocks": nb,
+                        "mean_h_critical": float(h_lo.mean())})
+            crit[name] = h_lo
+        res["wall_s"] = time.perf_counter() - t0
+        out[name] = res
+    if "fp64" in crit and "fp32split" in crit:
+        out["fp32_vs_fp64"] = {
+            "f_c_rel_diff": abs(out["fp32split"]["f_c"] - out["fp64"]["f_c"]) / out["fp64"]["f_c"],
+            "max_abs_h_diff_critical": float((crit["fp64"] - crit["fp32split"]).abs().max())}
+        # sweep rate: resident vs plain host-driven, one block at the last blocked force
+        p_lo = Q.Params(float(n), 1.0, out["fp64"]["f_lo"], Q.Model.Linear)
+        rates = {}
+        for form in (Q.QEW_RK_RESIDENT, Q.QEW_RK_PLAIN):
+            h = crit["fp64"].clone()
+            rpp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
+                             runaway=2.0 * ny, max_sweeps=args.dep_rate_sweeps)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = Q.rk_block(h, Q.Params(float(n), 1.0, out["fp64"]["f_c"], Q.Model.Linear), fld,
+                           rpp, form=form)
+            torch.cuda.synchronize()
+            rates["resident" if form == Q.QEW_RK_RESIDENT else "plain"] = \
+                r.sweeps / (time.perf_counter() - t0)
+        out["sweeps_per_s"] = rates
+    out["value"] = out["fp64"]["wall_s"]
+    return out
+
+
 # ---------------------------------------------------------------- our arm
 def timed(torch, fn, steps, ctx):
     """Run fn() `steps` times between CUDA events on the current stream;
@@ -404,11 +522,20 @@ def run_ours(args):
         e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
                "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
                "call": "qew_gradient_host (FP64 host heights in, FP64 host gradient out)"}
-    ensemble = None
-    if not args.profile_run and args.ensemble_lines > 0:
+    ensemble = dynamics = depinning = None
+    sections = set(s.strip() for s in args.sections.split(",") if s.strip())
+    if not args.profile_run and sections:
         del noise, cells, fracs, g32, g64, hs
         torch.cuda.empty_cache()
-        ensemble = run_ensemble(args, Q, torch)
+        if "ensemble" in sections and args.ensemble_lines > 0:
+            ensemble = run_ensemble(args, Q, torch)
+            torch.cuda.empty_cache()
+        if "dynamics" in sections:
+            dynamics = run_dynamics(args, Q, torch)
+            torch.cuda.empty_cache()
+        if "depinning" in sections:
+            depinning = run_depinning(args, Q, torch)
+            torch.cuda.empty_cache()
     if not args.profile_run:
         if rank == 0 and args.cpu_seconds > 0:
             cpu = cpu_gradient_rate(args.cpu_seconds)
@@ -430,7 +557,8 @@ def run_ours(args):
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "roofline": roof_split if headline_split else roof_fp64,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-                "other_precision": other, "ensemble": ensemble}
+                "other_precision": other, "ensemble": ensemble, "dynamics": dynamics,
+                "depinning": depinning}
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

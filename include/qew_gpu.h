@@ -315,6 +315,17 @@ qew_status qew_langevin_step_increments(qew_langevin *lgv,
                                         const qew_field *field, double *d_h,
                                         const qew_params *p, double drift,
                                         double diff, const double *d_xi);
+/* `steps` consecutive LangevinDynamics::step calls with per-step
+ * coefficients h_drift[k], h_diff[k] (host arrays): the anneal loop of
+ * dynamic_anneal (qew_runs.h:162-175) run in one cooperative persistent
+ * kernel, same increments as the step-by-step calls (the Philox step
+ * counter advances on each diff > 0 step). precision QEW_PREC_FP32_SPLIT
+ * gathers the FP32 coefficients and draws the normals with an FP32
+ * Box-Muller from the same Philox blocks; heights stay FP64. */
+qew_status qew_langevin_run(qew_langevin *lgv, const qew_field *field,
+                            double *d_h, const qew_params *p, int steps,
+                            const double *h_drift, const double *h_diff,
+                            int precision);
 /* The increments the next qew_langevin_step would use, without stepping. */
 qew_status qew_langevin_peek_increments(qew_langevin *lgv, double *d_xi);
 /* Steps taken so far (the Philox step counter). */
@@ -330,6 +341,18 @@ qew_status qew_rk_site_velocity(qew_ctx *ctx, const qew_field *field,
 qew_status qew_rk_block(qew_ctx *ctx, const qew_field *field, double *d_h,
                         int n, const qew_params *p, const qew_rk_params *rp,
                         qew_rk_result *res);
+/* rk_block forms: RESIDENT (the default of qew_rk_block) runs every sweep in
+ * one cooperative persistent kernel with device-side verdicts; PLAIN keeps
+ * the reference's host-driven loop (two colour kernels and one reduction
+ * read back per sweep). Both give bit-identical lines. */
+enum { QEW_RK_PLAIN = 0, QEW_RK_RESIDENT = 1 };
+/* rk_block with the form and the gather precision chosen: QEW_PREC_FP32_SPLIT
+ * (resident form only) evaluates site velocities on the FP32 coefficients
+ * while heights, the no-passing update and the verdicts stay FP64. */
+qew_status qew_rk_block_form(qew_ctx *ctx, const qew_field *field,
+                             double *d_h, int n, const qew_params *p,
+                             const qew_rk_params *rp, int form, int precision,
+                             qew_rk_result *res);
 /* Force bisection for f_c (no reference counterpart; the reference ramps,
  * qew_runs.h:226-241): from a blocked d_h at f_lo and an unblocked f_hi,
  * bisect f, restarting each rk_block from the last blocked configuration,
@@ -341,6 +364,14 @@ qew_status qew_depinning_bisect(qew_ctx *ctx, const qew_field *field,
                                 double f_hi, double rtol, int max_steps,
                                 double *f_c, double *f_lo_out,
                                 double *f_hi_out, int *n_blocks);
+/* The same bisection with the velocity precision chosen (QEW_PREC_*). */
+qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field,
+                                     double *d_h, int n, const qew_params *p,
+                                     const qew_rk_params *rp, double f_lo,
+                                     double f_hi, double rtol, int max_steps,
+                                     int precision, double *f_c,
+                                     double *f_lo_out, double *f_hi_out,
+                                     int *n_blocks);
 
 #ifdef __cplusplus
 }

@@ -36,7 +36,8 @@ from . import _capi
 from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # noqa: F401
                     QEW_FIELD_SINCOS, QEW_FIELD_WASHBOARD, QEW_FIELD_ZERO,
                     QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT, QEW_PREC_FP32_SPLIT,
-                    QEW_PREC_FP64, QEW_STORE_FP32, QEW_STORE_FP64, QewError)
+                    QEW_PREC_FP64, QEW_RK_PLAIN, QEW_RK_RESIDENT, QEW_STORE_FP32,
+                    QEW_STORE_FP64, QewError)
 
 __all__ = [
     "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
@@ -507,6 +508,18 @@ class LangevinDynamics:
             self.h, noise.h, _ptr(h), C.byref(pc), float(drift_coeff), float(diff_coeff),
             _ptr(xi)), self.ctx.h, "langevin step")
 
+    def run(self, h, p: Params, noise: _Noise, drift, diff, precision: int = QEW_PREC_FP64):
+        """len(drift) steps with per-step coefficients, in one device-resident launch."""
+        self.ctx.sync_stream()
+        drift = np.ascontiguousarray(drift, dtype=np.float64)
+        diff = np.ascontiguousarray(diff, dtype=np.float64)
+        if drift.shape != diff.shape or drift.ndim != 1 or h.numel() != self.n:
+            raise ValueError("schedule / line length mismatch")
+        pc = p.c()
+        _capi.check(self.ctx.lib.qew_langevin_run(
+            self.h, noise.h, _ptr(h), C.byref(pc), drift.size, drift.ctypes.data_as(_capi.PD),
+            diff.ctypes.data_as(_capi.PD), int(precision)), self.ctx.h, "langevin run")
+
     def peek_increments(self):
         torch = _torch()
         self.ctx.sync_stream()
@@ -541,27 +554,37 @@ def rk_site_velocity(h, p: Params, noise: _Noise):
     return out
 
 
-def rk_block(h, p: Params, noise: _Noise, rp: RkParams) -> RkResult:
-    """rk_block(h, p, noise, rp) (rosso_krauth.h:128-194); ValueError on odd n."""
+def rk_block(h, p: Params, noise: _Noise, rp: RkParams, form: int | None = None,
+             precision: int = QEW_PREC_FP64) -> RkResult:
+    """rk_block(h, p, noise, rp) (rosso_krauth.h:128-194); ValueError on odd n.
+
+    form: None (the library default, the resident kernel), QEW_RK_PLAIN or
+    QEW_RK_RESIDENT; precision QEW_PREC_FP32_SPLIT needs FP32 storage."""
     ctx = noise.ctx
     ctx.sync_stream()
     pc, rpc, res = p.c(), rp.c(), _capi.qew_rk_result()
-    _capi.check(ctx.lib.qew_rk_block(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
-                                     C.byref(rpc), C.byref(res)), ctx.h, "rk_block")
+    if form is None and precision == QEW_PREC_FP64:
+        st = ctx.lib.qew_rk_block(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc), C.byref(rpc),
+                                  C.byref(res))
+    else:
+        st = ctx.lib.qew_rk_block_form(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                       C.byref(rpc), _capi.QEW_RK_RESIDENT if form is None else
+                                       int(form), int(precision), C.byref(res))
+    _capi.check(st, ctx.h, "rk_block")
     return RkResult(bool(res.blocked), bool(res.runaway), res.sweeps, res.total_advance,
                     res.mean_h)
 
 
 def depinning_bisect(h, p: Params, noise: _Noise, rp: RkParams, f_lo: float, f_hi: float,
-                     rtol: float = 1e-10, max_steps: int = 200):
+                     rtol: float = 1e-10, max_steps: int = 200,
+                     precision: int = QEW_PREC_FP64):
     """Bisect the depinning force from a blocked h at f_lo; see qew_gpu.h."""
     ctx = noise.ctx
     ctx.sync_stream()
     pc, rpc = p.c(), rp.c()
     fc, flo, fhi, nb = C.c_double(), C.c_double(), C.c_double(), C.c_int()
-    _capi.check(ctx.lib.qew_depinning_bisect(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
-                                             C.byref(rpc), float(f_lo), float(f_hi), float(rtol),
-                                             int(max_steps), C.byref(fc), C.byref(flo),
-                                             C.byref(fhi), C.byref(nb)), ctx.h,
-                "depinning_bisect")
+    _capi.check(ctx.lib.qew_depinning_bisect_prec(
+        ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc), C.byref(rpc), float(f_lo), float(f_hi),
+        float(rtol), int(max_steps), int(precision), C.byref(fc), C.byref(flo), C.byref(fhi),
+        C.byref(nb)), ctx.h, "depinning_bisect")
     return fc.value, flo.value, fhi.value, nb.value

@@ -30,6 +30,7 @@ QEW_STORE_FP64, QEW_STORE_FP32 = 1, 2
 QEW_PREC_FP64, QEW_PREC_FP32_SPLIT = 0, 1
 QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
 QEW_NOALLOC_MAX_N = 1048576
+QEW_RK_PLAIN, QEW_RK_RESIDENT = 0, 1
 
 
 class qew_params(C.Structure):
@@ -114,6 +115,7 @@ _SIGS = {
     "qew_langevin_step": (I, [VP, VP, VP, C.POINTER(qew_params), D, D]),
     "qew_langevin_step_increments": (I, [VP, VP, VP, C.POINTER(qew_params), D, D, VP]),
     "qew_langevin_peek_increments": (I, [VP, VP]),
+    "qew_langevin_run": (I, [VP, VP, VP, C.POINTER(qew_params), I, PD, PD, I]),
     "qew_langevin_steps": (U64, [VP]),
     "qew_rk_site_velocity": (I, [VP, VP, VP, I, C.POINTER(qew_params), VP]),
     "qew_rk_block": (I, [VP, VP, VP, I, C.POINTER(qew_params), C.POINTER(qew_rk_params),
@@ -121,6 +123,11 @@ _SIGS = {
     "qew_depinning_bisect": (I, [VP, VP, VP, I, C.POINTER(qew_params),
                                  C.POINTER(qew_rk_params), D, D, D, I, PD, PD, PD,
                                  C.POINTER(I)]),
+    "qew_rk_block_form": (I, [VP, VP, VP, I, C.POINTER(qew_params), C.POINTER(qew_rk_params),
+                              I, I, C.POINTER(qew_rk_result)]),
+    "qew_depinning_bisect_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params),
+                                      C.POINTER(qew_rk_params), D, D, D, I, I, PD, PD, PD,
+                                      C.POINTER(I)]),
 }
 
 

@@ -7,10 +7,15 @@
 // independently (and by the oracle, bit-for-bit in the uniforms). Trajectory
 // parity with the reference is checked through the increments entry point,
 // which takes xi from the caller.
+#include <algorithm>
 #include <new>
+#include <type_traits>
+#include <vector>
 
+#include "qew_gridsync.cuh"
 #include "qew_internal.cuh"
 #include "qew_model_kernels.cuh"
+#include "qew_noise32.cuh"
 #include "qew_philox.cuh"
 
 struct qew_langevin {
@@ -59,6 +64,86 @@ __global__ void k_philox_fill(double *out, int n, uint64_t seed, uint64_t step) 
     philox_normal_pair(seed, step, (uint32_t)j, z0, z1);
     out[i0] = z0;
     if (i0 + 1 < n) out[i0 + 1] = z1;
+}
+
+// ---- many steps in one cooperative persistent kernel ----
+// The annealing loop of dynamic_anneal (qew_runs.h:162-175) on the device:
+// step k uses drift[k], diff[k] and Philox step index rstep[k]. Heights are
+// double-buffered (every gradient reads the previous step's line, as the
+// reference's gradient-then-update does), one bounded grid barrier per step.
+constexpr int kRunBS = 128;
+constexpr int kRunTile = 2 * kRunBS;  // a thread owns one site pair (one Philox block)
+
+// Box-Muller in FP32 from the same Philox block: 24-bit uniforms, FP32
+// log / sqrt / sincospi (the FP32-gather run's increments).
+__device__ __forceinline__ void philox_normal_pair_f32(uint64_t seed, uint64_t step, uint32_t j,
+                                                       double &z0, double &z1) {
+    uint32_t c[4] = {j, 0u, (uint32_t)step, (uint32_t)(step >> 32)};
+    philox4x32_10(c, seed);
+    const float u1 = ((float)(c[0] >> 8) + 1.0f) * (1.0f / 16777216.0f);
+    const float u2 = (float)(c[2] >> 8) * (1.0f / 16777216.0f);
+    const float r = sqrtf(-2.0f * logf(u1));
+    float s, co;
+    sincospif(2.0f * u2, &s, &co);
+    z0 = (double)(r * co);
+    z1 = (double)(r * s);
+}
+
+template <class Noise, bool NORMAL32>
+__global__ void __launch_bounds__(kRunBS)
+k_langevin_run(Noise nz, double *h, double *tmp, int n, LineDx L, double lt, double f, int model,
+               int steps, const double *__restrict__ drift, const double *__restrict__ diff,
+               const unsigned long long *__restrict__ rstep, uint64_t seed, GridSync *sync) {
+    __shared__ double s_h[kRunTile + 2];
+    __shared__ double s_dv[kRunTile + 1];
+    __shared__ double s_sl[kRunTile + 1];
+    const bool arc = (model == QEW_MODEL_ARCLENGTH);
+    const int t = threadIdx.x;
+    double *cur = h, *nxt = tmp;
+    for (int k = 0; k < steps; ++k) {
+        const double a = drift[k], b = diff[k];
+        const uint64_t rs = rstep[k];
+        for (int base = blockIdx.x * kRunTile; base < n; base += gridDim.x * kRunTile) {
+            const int cnt = min(kRunTile, n - base);
+            for (int j = t; j < cnt; j += kRunBS) s_h[j + 1] = __ldcg(cur + base + j);
+            if (t == 0) s_h[0] = __ldcg(cur + (base == 0 ? n - 1 : base - 1));
+            if (t == kRunBS - 1) s_h[cnt + 1] = __ldcg(cur + ((base + cnt == n) ? 0 : base + cnt));
+            __syncthreads();
+            for (int j = t; j < cnt; j += kRunBS)
+                edge_gradient(nz, base + j, n, s_h[j + 1], s_h[j + 2], L, arc, s_dv[j + 1], s_sl[j + 1]);
+            if (t == 0)
+                edge_gradient(nz, base == 0 ? n - 1 : base - 1, n, s_h[0], s_h[1], L, arc, s_dv[0],
+                              s_sl[0]);
+            __syncthreads();
+            const int j0 = 2 * t;
+            if (j0 < cnt) {
+                double z0 = 0.0, z1 = 0.0;
+                if (b > 0) {
+                    const uint32_t pair = (uint32_t)((base + j0) >> 1);
+                    if (NORMAL32)
+                        philox_normal_pair_f32(seed, rs, pair, z0, z1);
+                    else
+                        philox_normal_pair(seed, rs, pair, z0, z1);
+                }
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int j = j0 + q;
+                    if (j >= cnt) break;
+                    const double g = site_gradient(s_h[j], s_h[j + 1], s_h[j + 2], s_dv[j],
+                                                   s_dv[j + 1], s_sl[j], s_sl[j + 1], L, lt, f, arc);
+                    const double z = q ? z1 : z0;
+                    nxt[base + j] = (b > 0) ? s_h[j + 1] + (-a * g + b * z) : s_h[j + 1] + -a * g;
+                }
+            }
+            __syncthreads();
+        }
+        if (!grid_sync_bounded(sync, gridDim.x)) return;
+        double *sw = cur;
+        cur = nxt;
+        nxt = sw;
+    }
+    if (cur != h)
+        for (int i = blockIdx.x * kRunBS + t; i < n; i += gridDim.x * kRunBS) h[i] = __ldcg(cur + i);
 }
 
 qew_status check(qew_langevin *l, const qew_field *field, double *d_h, const qew_params *p) {
@@ -140,5 +225,73 @@ qew_status qew_langevin_peek_increments(qew_langevin *l, double *d_xi) {
 }
 
 uint64_t qew_langevin_steps(const qew_langevin *l) { return l ? l->step : 0; }
+
+qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h,
+                            const qew_params *p, int steps, const double *h_drift,
+                            const double *h_diff, int precision) {
+    QEW_TRY(check(l, field, d_h, p));
+    qew_ctx *ctx = l->ctx;
+    if (steps < 0 || (steps > 0 && (!h_drift || !h_diff)))
+        return qew_fail(ctx, QEW_ERR_INVALID, "langevin_run: bad schedule");
+    if (steps == 0) return QEW_OK;
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+    if (!coop) return qew_fail(ctx, QEW_ERR_UNSUPPORTED, "langevin_run: no cooperative launch");
+    const int n = l->n;
+    // Philox step index of each step: the counter advances on diff > 0 steps
+    std::vector<unsigned long long> rs(steps);
+    uint64_t c = l->step;
+    for (int k = 0; k < steps; ++k) {
+        rs[k] = c;
+        if (h_diff[k] > 0) ++c;
+    }
+    const size_t off_diff = ((size_t)steps * 8 + 255) & ~size_t(255);
+    const size_t off_rs = off_diff + (((size_t)steps * 8 + 255) & ~size_t(255));
+    const size_t off_tmp = off_rs + (((size_t)steps * 8 + 255) & ~size_t(255));
+    const size_t off_sync = off_tmp + (((size_t)n * 8 + 255) & ~size_t(255));
+    QEW_TRY(qew_scratch_reserve(ctx, off_sync + sizeof(GridSync) + 256));
+    char *base = (char *)ctx->scratch;
+    double *d_drift = (double *)base, *d_diff = (double *)(base + off_diff);
+    unsigned long long *d_rs = (unsigned long long *)(base + off_rs);
+    double *tmp = (double *)(base + off_tmp);
+    GridSync *sync = (GridSync *)(base + off_sync);
+    QEW_CUDA(ctx, cudaMemcpyAsync(d_drift, h_drift, (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
+    QEW_CUDA(ctx, cudaMemcpyAsync(d_diff, h_diff, (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
+    QEW_CUDA(ctx, cudaMemcpyAsync(d_rs, rs.data(), (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
+    QEW_CUDA(ctx, cudaMemsetAsync(sync, 0, sizeof(GridSync), ctx->stream));
+    LineDx L = make_line_dx(p->physical_size, n);
+    double lt = p->line_tension, fd = p->driving_force;
+    int model = p->model;
+    uint64_t seed = l->seed;
+    auto launch = [&](auto nz, auto normal32) -> qew_status {
+        auto kern = k_langevin_run<decltype(nz), decltype(normal32)::value>;
+        int per_sm = 0;
+        QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRunBS, 0));
+        const int want = (n + kRunTile - 1) / kRunTile;
+        const int grid = std::max(1, std::min(want, ctx->num_sms * std::max(per_sm, 1)));
+        void *args[] = {(void *)&nz, (void *)&d_h, (void *)&tmp, (void *)&n, (void *)&L,
+                        (void *)&lt, (void *)&fd, (void *)&model, (void *)&steps,
+                        (void *)&d_drift, (void *)&d_diff, (void *)&d_rs, (void *)&seed,
+                        (void *)&sync};
+        QEW_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kRunBS),
+                                                  args, 0, ctx->stream));
+        return qew_launch_check(ctx, "langevin_run");
+    };
+    if (precision == QEW_PREC_FP32_SPLIT) {
+        if (field->kind != QEW_FIELD_BSPLINE || !field->coef32)
+            return qew_fail(ctx, QEW_ERR_INVALID, "langevin_run: FP32 gather needs QEW_STORE_FP32");
+        QEW_TRY(launch(make_split32(field, n, p->physical_size), std::true_type{}));
+    } else {
+        QEW_TRY(qew_dispatch_noise(ctx, field, [&](auto nz) {
+            return launch(nz, std::false_type{});
+        }, n, p->physical_size));
+    }
+    GridSync hs;
+    QEW_CUDA(ctx, cudaMemcpyAsync(&hs, sync, sizeof(GridSync), cudaMemcpyDeviceToHost, ctx->stream));
+    QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hs.err) return qew_fail(ctx, QEW_ERR_TIMEOUT, "langevin_run: grid barrier timed out");
+    l->step = c;
+    return QEW_OK;
+}
 
 }  // extern "C"

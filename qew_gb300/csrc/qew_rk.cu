@@ -125,10 +125,40 @@ qew_status qew_rk_block(qew_ctx *ctx, const qew_field *field, double *d_h, int n
     return qew_rk_block_dispatch(ctx, field, d_h, n, p, rp, res);
 }
 
+qew_status qew_rk_block_form(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
+                             const qew_params *p, const qew_rk_params *rp, int form,
+                             int precision, qew_rk_result *res) {
+    if (!ctx || !field || !d_h || !res) return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: bad arguments");
+    QEW_TRY(qew_rk_validate(ctx, n, p, rp));
+    QEW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (form == QEW_RK_PLAIN) {
+        if (precision != QEW_PREC_FP64)
+            return qew_fail(ctx, QEW_ERR_UNSUPPORTED, "rk_block: the host-driven form is FP64 only");
+        return qew_rk_block_plain(ctx, field, d_h, n, p, rp, res);
+    }
+    if (form != QEW_RK_RESIDENT) return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: unknown form");
+    return qew_rk_block_resident(ctx, field, d_h, n, p, rp, precision, res);
+}
+
+qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
+                                     const qew_params *p, const qew_rk_params *rp, double f_lo,
+                                     double f_hi, double rtol, int max_steps, int precision,
+                                     double *f_c, double *f_lo_out, double *f_hi_out,
+                                     int *n_blocks);
+
 qew_status qew_depinning_bisect(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
                                 const qew_params *p, const qew_rk_params *rp, double f_lo,
                                 double f_hi, double rtol, int max_steps, double *f_c,
                                 double *f_lo_out, double *f_hi_out, int *n_blocks) {
+    return qew_depinning_bisect_prec(ctx, field, d_h, n, p, rp, f_lo, f_hi, rtol, max_steps,
+                                     QEW_PREC_FP64, f_c, f_lo_out, f_hi_out, n_blocks);
+}
+
+qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
+                                     const qew_params *p, const qew_rk_params *rp, double f_lo,
+                                     double f_hi, double rtol, int max_steps, int precision,
+                                     double *f_c, double *f_lo_out, double *f_hi_out,
+                                     int *n_blocks) {
     if (!ctx || !field || !d_h || !f_c || !(f_hi >= f_lo) || max_steps < 0)
         return qew_fail(ctx, QEW_ERR_INVALID, "depinning_bisect: bad arguments");
     QEW_TRY(qew_rk_validate(ctx, n, p, rp));
@@ -150,7 +180,9 @@ qew_status qew_depinning_bisect(qew_ctx *ctx, const qew_field *field, double *d_
         }
         pp.driving_force = fm;
         qew_rk_result r;
-        st = qew_rk_block_dispatch(ctx, field, work, n, &pp, rp, &r);
+        st = (precision == QEW_PREC_FP64) ? qew_rk_block_dispatch(ctx, field, work, n, &pp, rp, &r)
+                                          : qew_rk_block_resident(ctx, field, work, n, &pp, rp,
+                                                                  precision, &r);
         if (st != QEW_OK) break;
         ++steps;
         if (r.blocked) {

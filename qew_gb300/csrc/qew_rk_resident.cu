@@ -1,8 +1,148 @@
-// qew_rk_resident.cu -- form selection for rk_block.
+// qew_rk_resident.cu -- rk_block (rosso_krauth.h:128-194) as one persistent
+// cooperative kernel: all sweeps, both colours and the per-sweep verdict run
+// on the device, with a grid barrier between colours instead of a kernel
+// launch, and the sweep's total advance reduced deterministically (per-CTA
+// partials summed in CTA order by every CTA). The per-site arithmetic is
+// exactly the host-driven form's (qew_rk_device.cuh), so both forms produce
+// bit-identical lines.
+//
+// The grid barrier spins on a generation word with a bounded number of polls;
+// if it gives up it raises an error flag, every CTA leaves the sweep loop, and
+// the host returns QEW_ERR_TIMEOUT. A cooperative launch guarantees that all
+// CTAs are resident, so the barrier completes unless the device is stalled.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
+#include "qew_gridsync.cuh"
+#include "qew_internal.cuh"
+#include "qew_noise32.cuh"
+#include "qew_rk_device.cuh"
 #include "qew_rk_internal.cuh"
+
+namespace {
+
+constexpr int kRkBS = 128;
+template <class Noise>
+__global__ void __launch_bounds__(kRkBS)
+k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n, double dx,
+              double lt, double f, int model, RkP rp, double *partials, GridSync *sync,
+              qew_rk_result *out) {
+    const unsigned int nb = gridDim.x;
+    const int gtid = blockIdx.x * kRkBS + threadIdx.x;
+    const int gstride = nb * kRkBS;
+    const int half = n / 2;
+    __shared__ double s_w[kRkBS / 32];
+    // mean(h) at entry (rosso_krauth.h:144-148)
+    double acc = 0.0;
+    for (int i = gtid; i < n; i += gstride) acc += h[i];
+    acc = block_sum<kRkBS>(acc, s_w);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    if (!grid_sync_bounded(sync, nb)) return;
+    double mean_h0 = 0.0;
+    for (unsigned int b = 0; b < nb; ++b) mean_h0 += __ldcg(partials + b);
+    mean_h0 /= (double)n;
+
+    qew_rk_result res{};
+    double cum_adv = 0.0;
+    for (int sweep = 0; sweep < rp.max_sweeps; ++sweep) {
+        double local = 0.0;
+        for (int color = 0; color < 2; ++color) {
+            for (int k = gtid; k < half; k += gstride) {
+                const int i = 2 * k + color;
+                const int im = (i == 0) ? n - 1 : i - 1;
+                const int ip = (i + 1 == n) ? 0 : i + 1;
+                bool found = false;
+                const double hi = __ldcg(h + i);
+                const double hnew = rk_forward_zero(nz, i, n, dx, lt, f, model, hi, __ldcg(h + im),
+                                                    __ldcg(h + ip), rp, found);
+                const double a = hnew - hi;
+                adv[i] = a;
+                h[i] = hnew;
+                local += a;
+            }
+            if (color == 0 && !grid_sync_bounded(sync, nb)) return;
+        }
+        // sweep total: per-CTA partials (double-buffered by sweep parity)
+        double *part = partials + nb * (1 + (sweep & 1));
+        local = block_sum<kRkBS>(local, s_w);
+        if (threadIdx.x == 0) part[blockIdx.x] = local;
+        if (!grid_sync_bounded(sync, nb)) return;
+        double total_adv = 0.0;
+        for (unsigned int b = 0; b < nb; ++b) total_adv += __ldcg(part + b);
+        cum_adv += total_adv;
+        const double mean_adv = cum_adv / (double)n;
+        res.sweeps = sweep + 1;
+        res.total_advance = total_adv;
+        res.mean_h = mean_h0 + mean_adv;
+        if (mean_adv > rp.runaway) {
+            res.runaway = 1;
+            res.blocked = 0;
+            break;
+        }
+        if (total_adv < rp.sweep_tol) {
+            res.blocked = 1;
+            res.runaway = 0;
+            break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = res;
+}
+
+}  // namespace
+
+qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
+                                 const qew_params *p, const qew_rk_params *rp, int precision,
+                                 qew_rk_result *res) {
+    const double dx = p->physical_size / (double)n;
+    const RkP rk = rkp_from(rp);
+    int max_per_sm = 0;
+    auto launch = [&](auto nz) -> qew_status {
+        auto kern = k_rk_resident<decltype(nz)>;
+        QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, kern, kRkBS, 0));
+        const int want = (n / 2 + kRkBS - 1) / kRkBS;
+        const int grid = std::max(1, std::min(want, ctx->num_sms * std::max(max_per_sm, 1)));
+        // scratch: adv[n], partials[3*grid], sync word, result
+        const size_t off_part = ((size_t)n * sizeof(double) + 255) & ~size_t(255);
+        const size_t off_sync = (off_part + 3 * (size_t)grid * sizeof(double) + 255) & ~size_t(255);
+        const size_t off_res = (off_sync + sizeof(GridSync) + 255) & ~size_t(255);
+        QEW_TRY(qew_scratch_reserve(ctx, off_res + sizeof(qew_rk_result) + 256));
+        char *base = (char *)ctx->scratch;
+        double *adv = (double *)base;
+        double *part = (double *)(base + off_part);
+        GridSync *sync = (GridSync *)(base + off_sync);
+        qew_rk_result *d_res = (qew_rk_result *)(base + off_res);
+        QEW_CUDA(ctx, cudaMemsetAsync(adv, 0, (size_t)n * sizeof(double), ctx->stream));
+        QEW_CUDA(ctx, cudaMemsetAsync(sync, 0, sizeof(GridSync), ctx->stream));
+        double lt = p->line_tension, fd = p->driving_force;
+        int model = p->model;
+        void *args[] = {(void *)&nz, (void *)&d_h, (void *)&adv, (void *)&n, (void *)&dx,
+                        (void *)&lt, (void *)&fd, (void *)&model, (void *)&rk, (void *)&part,
+                        (void *)&sync, (void *)&d_res};
+        QEW_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kRkBS), args,
+                                                  0, ctx->stream));
+        QEW_TRY(qew_launch_check(ctx, "rk_resident"));
+        GridSync hs;
+        QEW_CUDA(ctx, cudaMemcpyAsync(res, d_res, sizeof(qew_rk_result), cudaMemcpyDeviceToHost,
+                                      ctx->stream));
+        QEW_CUDA(ctx, cudaMemcpyAsync(&hs, sync, sizeof(GridSync), cudaMemcpyDeviceToHost, ctx->stream));
+        QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if (hs.err) return qew_fail(ctx, QEW_ERR_TIMEOUT, "rk_block: grid barrier timed out");
+        return QEW_OK;
+    };
+    if (precision == QEW_PREC_FP32_SPLIT) {
+        if (field->kind != QEW_FIELD_BSPLINE || !field->coef32)
+            return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: FP32 storage needs QEW_STORE_FP32");
+        return launch(make_split32(field, n, p->physical_size));
+    }
+    return qew_dispatch_noise(ctx, field, launch, n, p->physical_size);
+}
 
 qew_status qew_rk_block_dispatch(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
                                  const qew_params *p, const qew_rk_params *rp,
                                  qew_rk_result *res) {
-    return qew_rk_block_plain(ctx, field, d_h, n, p, rp, res);
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+    if (!coop) return qew_rk_block_plain(ctx, field, d_h, n, p, rp, res);
+    return qew_rk_block_resident(ctx, field, d_h, n, p, rp, QEW_PREC_FP64, res);
 }

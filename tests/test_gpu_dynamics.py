@@ -114,3 +114,47 @@ def test_equipartition(Q):
             es.append(Q.objective(h, p, well))
     mean_e = float(np.mean(es))
     assert abs(mean_e - 0.5 * n * kT) < 0.1 * 0.5 * n * kT, mean_e
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_resident_run_matches_step_loop(Q, model):
+    """qew_langevin_run == the same schedule stepped one call at a time
+    (same Philox increments; FP64 within 1e-12 relative)."""
+    n, ny, Lx, Ly = 1000, 64, 100.0, 6.4
+    f = Q.FilteredNoise(band_limited_field(n, ny, Lx, Ly, 1.0, 0.4, 3), Lx, Ly)
+    p = Q.Params(Lx, 1.0, 0.3, Q.Model(model))
+    rng = np.random.default_rng(2)
+    h0 = 3.2 + 0.1 * rng.standard_normal(n)
+    steps = 301
+    drift = np.full(steps, 0.01)
+    diff = np.sqrt(2 * np.linspace(0.4, 0.0, steps) * 0.01)
+    diff[::7] = 0.0
+    d1, d2 = Q.LangevinDynamics(n, 5), Q.LangevinDynamics(n, 5)
+    h1, h2 = t64(h0), t64(h0)
+    for k in range(steps):
+        d1.step(h1, p, f, drift[k], diff[k])
+    d2.run(h2, p, f, drift, diff)
+    assert d1.steps == d2.steps
+    a, b = npy(h1), npy(h2)
+    assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(a))
+
+
+def test_resident_run_fp32(Q):
+    """FP32-gather run: deterministic part close to FP64, FP32 normals N(0,1)."""
+    n, ny = 4096, 64
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    f = Q.FilteredNoise(band_limited_field(n, ny, float(n), float(ny), 1.0, 4.0, 8),
+                        float(n), float(ny), store=store)
+    p = Q.Params(float(n), 1.0, 0.2, Q.Model.Arclength)
+    h0 = 32 + np.cumsum(np.random.default_rng(1).standard_normal(n)) * 0.01
+    a, b = t64(h0), t64(h0)
+    sched = np.full(200, 0.05)
+    Q.LangevinDynamics(n, 1).run(a, p, f, sched, np.zeros(200))
+    Q.LangevinDynamics(n, 1).run(b, p, f, sched, np.zeros(200), precision=Q.QEW_PREC_FP32_SPLIT)
+    assert np.max(np.abs(npy(a) - npy(b))) < 1e-4
+    zero = Q.FilteredNoise(np.zeros((n, ny)), float(n), float(ny), store=store)
+    h = t64(np.zeros(n))
+    Q.LangevinDynamics(n, 9).run(h, Q.Params(float(n), 0.0, 0.0), zero, [0.0], [1.0],
+                                 precision=Q.QEW_PREC_FP32_SPLIT)
+    z = npy(h)
+    assert abs(z.mean()) < 0.05 and abs(z.std() - 1.0) < 0.05

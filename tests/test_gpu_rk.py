@@ -136,3 +136,47 @@ def test_bisect_matches_oracle(Q, O):
                                                 1e-6, 60)
     assert abs(fc - fco) <= 1e-6 * fco
     assert np.max(np.abs(npy(h) - ho)) < 1e-6
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_resident_equals_plain_bitwise(Q, model):
+    """The persistent kernel and the host-driven loop run the same per-site
+    arithmetic: identical lines and verdicts."""
+    nx, ny, Lx, Ly = 128, 64, 6.4, 1.0
+    f = Q.FilteredNoise(band_limited_field(nx, ny, Lx, Ly, 0.6, 0.2, 31), Lx, Ly)
+    rp = rkp(Q, 0.5 / ny, Ly, 1e-11, 1e-9, 3 * Ly)
+    for fdr in (0.0, 0.25, 5.0):
+        p = Q.Params(Lx, 1.1, fdr, Q.Model(model))
+        h1, h2 = t64(np.full(nx, 0.5)), t64(np.full(nx, 0.5))
+        r1 = Q.rk_block(h1, p, f, rp, form=Q.QEW_RK_PLAIN)
+        r2 = Q.rk_block(h2, p, f, rp, form=Q.QEW_RK_RESIDENT)
+        assert (r1.blocked, r1.runaway, r1.sweeps) == (r2.blocked, r2.runaway, r2.sweeps)
+        assert np.array_equal(npy(h1), npy(h2))
+
+
+def test_fp32_velocity_form_close_to_fp64(Q):
+    nx, ny, Lx, Ly = 256, 64, 12.8, 1.0
+    f = Q.FilteredNoise(band_limited_field(nx, ny, Lx, Ly, 0.5, 0.2, 5), Lx, Ly,
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    rp = rkp(Q, 0.5 / ny, Ly, 1e-10, 1e-8, 3 * Ly)
+    p = Q.Params(Lx, 1.0, 0.1, Q.Model.Linear)
+    h64, h32 = t64(np.full(nx, 0.5)), t64(np.full(nx, 0.5))
+    r64 = Q.rk_block(h64, p, f, rp)
+    r32 = Q.rk_block(h32, p, f, rp, precision=Q.QEW_PREC_FP32_SPLIT)
+    assert r64.blocked and r32.blocked
+    assert np.max(np.abs(npy(h64) - npy(h32))) < 1e-4
+
+
+def test_bisect_fp32_close_to_fp64(Q):
+    nx, ny, Lx, Ly = 64, 64, 3.2, 1.0
+    f = Q.FilteredNoise(band_limited_field(nx, ny, Lx, Ly, 0.5, 0.2, 7), Lx, Ly,
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    rp = rkp(Q, 0.5 / ny, Ly, 1e-11, 1e-9, 3 * Ly, 50000)
+    p = Q.Params(Lx, 1.0, 0.0, Q.Model.Linear)
+    ha, hb = t64(np.full(nx, 0.5)), t64(np.full(nx, 0.5))
+    assert Q.rk_block(ha, p, f, rp).blocked
+    hb.copy_(ha)
+    fa = Q.depinning_bisect(ha, p, f, rp, 0.0, 4.0, rtol=1e-6, max_steps=60)[0]
+    fb = Q.depinning_bisect(hb, p, f, rp, 0.0, 4.0, rtol=1e-6, max_steps=60,
+                            precision=Q.QEW_PREC_FP32_SPLIT)[0]
+    assert abs(fa - fb) < 1e-4 * fa
