@@ -56,18 +56,33 @@ def parse():
                     help="lines of the batched-statics section (0 skips it)")
     ap.add_argument("--ensemble-ref", type=int, default=16,
                     help="lines timed with the plain one-line-per-launch form")
-    ap.add_argument("--sections", default="ensemble,dynamics,depinning",
+    ap.add_argument("--sections", default="ensemble,dynamics,depinning,serving",
                     help="extra configurations reported beside the headline")
     ap.add_argument("--dyn-steps", type=int, default=100000)
     ap.add_argument("--dyn-plain-steps", type=int, default=2000)
-    ap.add_argument("--dep-size", type=int, default=16384)
+    ap.add_argument("--dep-size", type=int, default=2048,
+                    help="line length and field size of the depinning section (16384: C2)")
+    ap.add_argument("--dep-max-sweeps", type=int, default=20000,
+                    help="RkParams::max_sweeps of the depinning section (200000: C2)")
     ap.add_argument("--dep-fstep", type=float, default=0.05)
     ap.add_argument("--dep-fmax", type=float, default=20.0)
     ap.add_argument("--dep-rate-sweeps", type=int, default=2000)
+    ap.add_argument("--serve-rates", default="100,300,1000,3000,10000")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-inflight", type=int, default=32)
+    ap.add_argument("--serve-lsteps", type=int, default=10000)
     return ap.parse_args()
 
 
 # ----------------------------------------------------------------- helpers
+_T0 = time.time()
+
+
+def log(msg: str) -> None:
+    """Progress to stderr (the JSON result line goes to stdout)."""
+    print("[bench %7.1fs] %s" % (time.time() - _T0, msg), file=sys.stderr, flush=True)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -346,7 +361,7 @@ def run_depinning(args, Q, torch):
     store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
     fld = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2, store=store)
     rp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
-                    runaway=2.0 * ny, max_sweeps=200000)
+                    runaway=2.0 * ny, max_sweeps=args.dep_max_sweeps)
     out = {"metric": "time to f_c (ramp + bisection to 1e-10)", "unit": "s",
            "workload": "L=%d, %dx%d field xi=4, linear, Gamma=1, f_step=%g" % (n, n, ny, args.dep_fstep)}
     crit = {}
@@ -361,6 +376,7 @@ def run_depinning(args, Q, torch):
             r = Q.rk_block(h, Q.Params(float(n), 1.0, fk, Q.Model.Linear), fld, rp, precision=prec)
             sweeps += r.sweeps
             blocks += 1
+            log("  depinning %s f=%.3f blocked=%d sweeps=%d" % (name, fk, r.blocked, r.sweeps))
             if not r.blocked:
                 f_hi = fk
                 break
@@ -397,6 +413,68 @@ def run_depinning(args, Q, torch):
                 r.sweeps / (time.perf_counter() - t0)
         out["sweeps_per_s"] = rates
     out["value"] = out["fp64"]["wall_s"]
+    return out
+
+
+# ------------------------------------------------------------- serving (C4)
+def run_serving(args, Q, torch):
+    """Poisson request streams (seed 4) at each rate: 50% static minimise
+    (FP64-refined to max|g| < 1e-8), 30% Langevin (serve_lsteps steps, T ~
+    U[0, 0.5], dt 0.01), 20% depinning f_c (ramp 0.05, bisection to 1e-3,
+    2000 sweeps per block); L log-uniform in [512, 65536] (even), 256 or 1024
+    rows, xi ~ U[2, 8]; each field generated on the device per request;
+    admission by a 150 GB HBM budget; continuous batching over
+    serve_inflight workers."""
+    rng = np.random.default_rng(4)
+    rates = [float(x) for x in args.serve_rates.split(",") if x]
+    srv = Q.Server(hbm_budget_bytes=150e9, max_inflight=args.serve_inflight)
+    out = {"metric": "serving latency p50/p99 and solves/s", "unit": "s",
+           "budget_GB": 150, "inflight": args.serve_inflight, "rates": [],
+           "mix": "50% static (1e-8), 30% Langevin (%d steps), 20%% depinning f_c"
+                  % args.serve_lsteps}
+    try:
+        for ri, rate in enumerate(rates):
+            N = args.serve_requests
+            reqs = []
+            for k in range(N):
+                kind = int(rng.choice(3, p=[0.5, 0.3, 0.2]))
+                n = int(round(np.exp(rng.uniform(np.log(512), np.log(65536))) / 2)) * 2
+                r = dict(kind=kind, n=n, rows=int(rng.choice([256, 1024])),
+                         xi=float(rng.uniform(2, 8)), seed=100000 * (ri + 1) + k,
+                         model=int(rng.integers(0, 2)))
+                if kind == 1:
+                    r.update(steps=args.serve_lsteps, temperature=float(rng.uniform(0, 0.5)),
+                             dt=0.01)
+                elif kind == 2:
+                    r.update(model=0, f_step=0.05, f_max=5.0, bisect_rtol=1e-3, max_sweeps=2000,
+                             max_advance=32.0, runaway=float(r["rows"]) / 4)
+                reqs.append(r)
+            gaps = rng.exponential(1.0 / rate, N)
+            t_next = srv.clock()
+            for k in range(N):
+                t_next += gaps[k]
+                while srv.clock() < t_next:
+                    time.sleep(min(1e-3, max(0.0, t_next - srv.clock())))
+                srv.submit(**reqs[k])
+            srv.drain(3600)
+            resps = srv.poll(N + 16)
+            log("  serving rate %g: %d responses" % (rate, len(resps)))
+            lat = np.array([r["t_end"] - r["t_submit"] for r in resps])
+            span = max(r["t_end"] for r in resps) - min(r["t_submit"] for r in resps)
+            per_kind = {}
+            for kind, name in ((0, "static"), (1, "langevin"), (2, "depinning")):
+                lk = [r["t_end"] - r["t_submit"] for r in resps if r["kind"] == kind]
+                if lk:
+                    per_kind[name] = {"count": len(lk), "p50_s": float(np.percentile(lk, 50)),
+                                      "p99_s": float(np.percentile(lk, 99))}
+            out["rates"].append({
+                "rate_per_s": rate, "requests": N, "ok": int(sum(r["status"] == 0 for r in resps)),
+                "static_converged_1e8": int(sum(r["kind"] == 0 and r["converged"] and
+                                                r["max_force"] < 1e-8 for r in resps)),
+                "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                "solves_per_s": N / span, "per_kind": per_kind})
+    finally:
+        srv.close()
     return out
 
 
@@ -522,20 +600,27 @@ def run_ours(args):
         e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
                "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
                "call": "qew_gradient_host (FP64 host heights in, FP64 host gradient out)"}
-    ensemble = dynamics = depinning = None
+    ensemble = dynamics = depinning = serving = None
     sections = set(s.strip() for s in args.sections.split(",") if s.strip())
     if not args.profile_run and sections:
         del noise, cells, fracs, g32, g64, hs
         torch.cuda.empty_cache()
         if "ensemble" in sections and args.ensemble_lines > 0:
+            log("ensemble section")
             ensemble = run_ensemble(args, Q, torch)
             torch.cuda.empty_cache()
         if "dynamics" in sections:
+            log("dynamics section")
             dynamics = run_dynamics(args, Q, torch)
             torch.cuda.empty_cache()
         if "depinning" in sections:
+            log("depinning section")
             depinning = run_depinning(args, Q, torch)
             torch.cuda.empty_cache()
+        if "serving" in sections:
+            log("serving section")
+            serving = run_serving(args, Q, torch)
+            log("serving done")
     if not args.profile_run:
         if rank == 0 and args.cpu_seconds > 0:
             cpu = cpu_gradient_rate(args.cpu_seconds)
@@ -558,7 +643,7 @@ def run_ours(args):
                 "roofline": roof_split if headline_split else roof_fp64,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "other_precision": other, "ensemble": ensemble, "dynamics": dynamics,
-                "depinning": depinning}
+                "depinning": depinning, "serving": serving}
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

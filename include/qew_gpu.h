@@ -299,6 +299,63 @@ qew_status qew_ensemble_minimize(qew_ctx *ctx, int count,
                                  const qew_ensemble_params *ep,
                                  qew_lbfgs_result *results);
 
+/* ---------------------------------------------------------------- serving */
+/* Continuous-batching server (no reference counterpart: the reference runs
+ * one simulation per process, via its three executables). Requests wait in a
+ * FIFO queue; `max_inflight` workers, each on its own CUDA stream, admit the
+ * queue head as soon as its device-memory estimate fits in the HBM budget
+ * left by the requests in flight, so new requests start while others run and
+ * their kernels overlap. Each request generates its own field on the device
+ * (qew_field_create_generated: n columns x rows rows, correlation xi cells,
+ * unit variance, `seed`) and keeps all state device-resident. Results depend
+ * only on the request: the same alone and in the mix. */
+typedef struct qew_server qew_server;
+enum { QEW_REQ_STATIC = 0, QEW_REQ_LANGEVIN = 1, QEW_REQ_DEPINNING = 2 };
+typedef struct {
+    int kind;              /* QEW_REQ_* */
+    int n;                 /* line points = field columns, grid spacing 1 */
+    int rows;              /* field rows */
+    double xi;             /* field correlation length, cells */
+    uint64_t seed;         /* field seed (Langevin increments: seed + 1) */
+    int model;             /* QEW_MODEL_* (depinning: linear) */
+    double line_tension;
+    double driving_force;  /* static and Langevin */
+    double ftol;           /* static: FP64 max|g| target (FP32 phase to 2e-5,
+                              then FP64 refinement, preconditioned, m = 10) */
+    int steps;             /* Langevin: steps at constant temperature */
+    double temperature;    /* Langevin: kT; drift = dt, diff = sqrt(2 T dt) */
+    double dt;
+    double f_step, f_max;  /* depinning: force ramp (qew_runs.h:224-241) */
+    double bisect_rtol;    /* depinning: f_c bisection tolerance */
+    int max_sweeps;        /* depinning: RkParams::max_sweeps */
+    double max_advance;    /* depinning: march cap per sweep, cells (<= 0: rows) */
+    double runaway;        /* depinning: runaway mean advance, cells (<= 0: 2 rows) */
+    double *h_out;         /* optional host buffer (n doubles) for the line */
+} qew_request;
+typedef struct {
+    uint64_t id;
+    int kind;
+    qew_status status;
+    double t_submit, t_start, t_end;  /* seconds on the server clock */
+    int iterations;  /* static: L-BFGS iterations; Langevin: steps;
+                        depinning: rk_block calls */
+    double value;    /* static: energy; Langevin: mean height; depinning: f_c
+                        (-1 if the ramp found no unblocked force) */
+    double max_force;/* static: final max|g| */
+    int converged;
+} qew_response;
+qew_status qew_server_create(int device, double hbm_budget_bytes,
+                             int max_inflight, qew_server **out);
+/* QEW_ERR_NOMEM if the request could never fit the budget. */
+qew_status qew_server_submit(qew_server *s, const qew_request *req,
+                             uint64_t *id);
+/* Moves up to `max` finished responses into out; returns how many. */
+int qew_server_poll(qew_server *s, qew_response *out, int max);
+/* Waits until the queue is empty and nothing runs (QEW_ERR_TIMEOUT). */
+qew_status qew_server_drain(qew_server *s, double timeout_s);
+double qew_server_clock(const qew_server *s);
+qew_status qew_server_destroy(qew_server *s);
+
 /* --------------------------------------------------------------- Langevin */
 /* LangevinDynamics(n, seed), dynamics.h:31-32. Increments are N(0,1) from a
  * Philox4x32-10 counter stream keyed by seed, counter (site pair, step). */

@@ -46,7 +46,7 @@ __all__ = [
     "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "ensemble_minimize",
     "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
-    "depinning_bisect", "Context", "default_context", "QewError",
+    "depinning_bisect", "Context", "default_context", "QewError", "Server",
 ]
 
 
@@ -588,3 +588,60 @@ def depinning_bisect(h, p: Params, noise: _Noise, rp: RkParams, f_lo: float, f_h
         float(rtol), int(max_steps), int(precision), C.byref(fc), C.byref(flo), C.byref(fhi),
         C.byref(nb)), ctx.h, "depinning_bisect")
     return fc.value, flo.value, fhi.value, nb.value
+
+
+# ---------------------------------------------------------------- serving
+class Server:
+    """Continuous-batching server over the C ABI (see qew_server_* in qew_gpu.h)."""
+
+    def __init__(self, hbm_budget_bytes: float = 150e9, max_inflight: int = 32,
+                 device: int | None = None):
+        torch = _torch()
+        self.lib = _capi.load()
+        self.device = torch.cuda.current_device() if device is None else device
+        h = C.c_void_p()
+        _capi.check(self.lib.qew_server_create(self.device, float(hbm_budget_bytes),
+                                               int(max_inflight), C.byref(h)), None,
+                    "qew_server_create")
+        self.h = h
+
+    def submit(self, kind: int, n: int, rows: int, xi: float, seed: int, *, model: int = 0,
+               line_tension: float = 1.0, driving_force: float = 0.0, ftol: float = 1e-8,
+               steps: int = 10000, temperature: float = 0.0, dt: float = 0.01,
+               f_step: float = 0.1, f_max: float = 10.0, bisect_rtol: float = 1e-10,
+               max_sweeps: int = 200000, max_advance: float = 0.0, runaway: float = 0.0,
+               h_out: np.ndarray | None = None) -> int:
+        r = _capi.qew_request(int(kind), int(n), int(rows), float(xi), int(seed), int(model),
+                              float(line_tension), float(driving_force), float(ftol), int(steps),
+                              float(temperature), float(dt), float(f_step), float(f_max),
+                              float(bisect_rtol), int(max_sweeps), float(max_advance),
+                              float(runaway),
+                              None if h_out is None else C.c_void_p(h_out.ctypes.data))
+        rid = C.c_uint64()
+        _capi.check(self.lib.qew_server_submit(self.h, C.byref(r), C.byref(rid)), None,
+                    "qew_server_submit")
+        return rid.value
+
+    def poll(self, max_items: int = 1024) -> list:
+        buf = (_capi.qew_response * max_items)()
+        k = self.lib.qew_server_poll(self.h, buf, max_items)
+        return [dict(id=b.id, kind=b.kind, status=b.status, t_submit=b.t_submit,
+                     t_start=b.t_start, t_end=b.t_end, iterations=b.iterations, value=b.value,
+                     max_force=b.max_force, converged=bool(b.converged)) for b in buf[:k]]
+
+    def drain(self, timeout_s: float = 600.0) -> None:
+        _capi.check(self.lib.qew_server_drain(self.h, float(timeout_s)), None, "drain")
+
+    def clock(self) -> float:
+        return float(self.lib.qew_server_clock(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.qew_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -31,6 +31,7 @@ QEW_PREC_FP64, QEW_PREC_FP32_SPLIT = 0, 1
 QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
 QEW_NOALLOC_MAX_N = 1048576
 QEW_RK_PLAIN, QEW_RK_RESIDENT = 0, 1
+QEW_REQ_STATIC, QEW_REQ_LANGEVIN, QEW_REQ_DEPINNING = 0, 1, 2
 
 
 class qew_params(C.Structure):
@@ -65,6 +66,20 @@ class qew_ensemble_line(C.Structure):
 
 class qew_ensemble_params(C.Structure):
     _fields_ = [("lbfgs", qew_lbfgs_params), ("ftol_fp32", D), ("max_iter_fp32", I)]
+
+
+class qew_request(C.Structure):
+    _fields_ = [("kind", I), ("n", I), ("rows", I), ("xi", D), ("seed", U64), ("model", I),
+                ("line_tension", D), ("driving_force", D), ("ftol", D), ("steps", I),
+                ("temperature", D), ("dt", D), ("f_step", D), ("f_max", D),
+                ("bisect_rtol", D), ("max_sweeps", I), ("max_advance", D), ("runaway", D),
+                ("h_out", VP)]
+
+
+class qew_response(C.Structure):
+    _fields_ = [("id", U64), ("kind", I), ("status", I), ("t_submit", D), ("t_start", D),
+                ("t_end", D), ("iterations", I), ("value", D), ("max_force", D),
+                ("converged", I)]
 
 
 class QewError(RuntimeError):
@@ -110,6 +125,12 @@ _SIGS = {
     "qew_precond_apply": (I, [VP, VP, I, D, D, D, I, VP]),
     "qew_ensemble_minimize": (I, [VP, I, C.POINTER(qew_ensemble_line),
                                   C.POINTER(qew_ensemble_params), C.POINTER(qew_lbfgs_result)]),
+    "qew_server_create": (I, [I, D, I, C.POINTER(VP)]),
+    "qew_server_submit": (I, [VP, C.POINTER(qew_request), C.POINTER(U64)]),
+    "qew_server_poll": (I, [VP, C.POINTER(qew_response), I]),
+    "qew_server_drain": (I, [VP, D]),
+    "qew_server_clock": (D, [VP]),
+    "qew_server_destroy": (I, [VP]),
     "qew_langevin_create": (I, [VP, I, U64, C.POINTER(VP)]),
     "qew_langevin_destroy": (I, [VP]),
     "qew_langevin_step": (I, [VP, VP, VP, C.POINTER(qew_params), D, D]),

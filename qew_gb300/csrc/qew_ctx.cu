@@ -16,19 +16,29 @@ qew_status qew_fail(qew_ctx *ctx, qew_status s, const char *fmt, ...) {
     return s;
 }
 
+qew_status qew_alloc_async(qew_ctx *ctx, void **p, size_t bytes) {
+    *p = nullptr;
+    if (cudaMallocAsync(p, bytes ? bytes : 1, ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return qew_fail(ctx, QEW_ERR_NOMEM, "cudaMallocAsync(%zu) failed", bytes);
+    }
+    return QEW_OK;
+}
+
+void qew_free_async(void *p, cudaStream_t stream) {
+    if (p) cudaFreeAsync(p, stream);
+}
+
 qew_status qew_scratch_reserve(qew_ctx *ctx, size_t bytes) {
     if (bytes <= ctx->scratch_bytes) return QEW_OK;
-    // keep the work already queued on the old buffer safe before freeing it
-    QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (ctx->scratch) cudaFree(ctx->scratch);
+    // stream-ordered: the old buffer is released after the work queued on it
+    if (ctx->scratch) qew_free_async(ctx->scratch, ctx->stream);
     ctx->scratch = nullptr;
     ctx->scratch_bytes = 0;
     size_t want = bytes + (bytes >> 2);
     want = (want + 255) & ~size_t(255);
-    if (cudaMalloc(&ctx->scratch, want) != cudaSuccess) {
-        cudaGetLastError();
-        return qew_fail(ctx, QEW_ERR_NOMEM, "scratch: cudaMalloc(%zu) failed", want);
-    }
+    QEW_TRY(qew_alloc_async(ctx, &ctx->scratch, want));
     ctx->scratch_bytes = want;
     return QEW_OK;
 }
@@ -39,6 +49,18 @@ qew_status qew_launch_check(qew_ctx *ctx, const char *what, int k) {
         return qew_fail(ctx, QEW_ERR_CUDA, "launch %s: %s", what, cudaGetErrorString(e));
     ctx->launches += (uint64_t)k;
     return QEW_OK;
+}
+
+// Let the device's default memory pool keep up to 16 GiB of freed blocks for
+// reuse (stream-ordered allocations of per-request buffers then stay cheap);
+// the setting lives in this process only.
+static bool keep_pool_cache(int device) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) != cudaSuccess) return true;
+    uint64_t threshold = 16ull << 30;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    cudaGetLastError();
+    return true;
 }
 
 extern "C" {
@@ -74,6 +96,7 @@ qew_status qew_ctx_create(int device, qew_ctx **out) {
         cudaMalloc(&ctx->red_out, sizeof(double) * 8) != cudaSuccess ||
         cudaMallocHost(&ctx->host_out, sizeof(double) * 8) != cudaSuccess ||
         cudaMemset(ctx->red_counter, 0, sizeof(unsigned int) * 8) != cudaSuccess ||
+        !keep_pool_cache(device) ||
         cudaDeviceSynchronize() != cudaSuccess) {
         cudaGetLastError();
         qew_ctx_destroy(ctx);
@@ -91,14 +114,19 @@ qew_status qew_ctx_destroy(qew_ctx *ctx) {
     if (ctx->red_counter) cudaFree(ctx->red_counter);
     if (ctx->red_out) cudaFree(ctx->red_out);
     if (ctx->host_out) cudaFreeHost(ctx->host_out);
-    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
     delete ctx;
     return QEW_OK;
 }
 
 qew_status qew_ctx_set_stream(qew_ctx *ctx, void *cuda_stream) {
     if (!ctx) return QEW_ERR_INVALID;
-    ctx->stream = (cudaStream_t)cuda_stream;
+    if ((cudaStream_t)cuda_stream != ctx->stream) {
+        // the scratch arena is stream-ordered on the old stream: drain it first
+        QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        ctx->stream = (cudaStream_t)cuda_stream;
+    }
     return QEW_OK;
 }
 

@@ -211,18 +211,18 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
     f->dx = Lx / nx;  // filtered_noise.cpp:87
     f->dy = Ly / ny;
     double *tmp = nullptr, *c64 = nullptr;
+    f->stream = ctx->stream;
     auto cleanup = [&](qew_status s) {
-        if (tmp) cudaFree(tmp);
-        if (c64) cudaFree(c64);
-        if (f->coef32) cudaFree(f->coef32);
+        qew_free_async(tmp, ctx->stream);
+        qew_free_async(c64, ctx->stream);
+        qew_free_async(f->coef32, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
         delete f;
         return s;
     };
-    if (cudaMalloc(&tmp, N * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&c64, N * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError();
-        return cleanup(qew_fail(ctx, QEW_ERR_NOMEM, "field_create: cudaMalloc of %zu bytes", 2 * N * 8));
-    }
+    if (qew_alloc_async(ctx, (void **)&tmp, N * sizeof(double)) != QEW_OK ||
+        qew_alloc_async(ctx, (void **)&c64, N * sizeof(double)) != QEW_OK)
+        return cleanup(QEW_ERR_NOMEM);
     cudaError_t e = cudaMemcpyAsync(tmp, src, N * sizeof(double),
                                     src_on_device ? cudaMemcpyDeviceToDevice
                                                   : cudaMemcpyHostToDevice,
@@ -239,11 +239,8 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
     st = prefilter_axis(ctx, c64, tmp, ny, nx, nx, 1);
     if (st != QEW_OK) return cleanup(st);
     if (store & QEW_STORE_FP32) {
-        if (cudaMalloc(&f->coef32, N * sizeof(float)) != cudaSuccess) {
-            cudaGetLastError();
-            f->coef32 = nullptr;
-            return cleanup(qew_fail(ctx, QEW_ERR_NOMEM, "field_create: FP32 copy"));
-        }
+        if (qew_alloc_async(ctx, (void **)&f->coef32, N * sizeof(float)) != QEW_OK)
+            return cleanup(QEW_ERR_NOMEM);
         const int blocks = ctx->num_sms * 8;
         k_to_fp32<<<blocks, 256, 0, ctx->stream>>>(c64, f->coef32, N);
         st = qew_launch_check(ctx, "to_fp32");
@@ -251,12 +248,12 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
     }
     e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "field build: %s", cudaGetErrorString(e)));
-    cudaFree(tmp);
+    qew_free_async(tmp, ctx->stream);
     tmp = nullptr;
     if (store & QEW_STORE_FP64) {
         f->coef64 = c64;
     } else {
-        cudaFree(c64);
+        qew_free_async(c64, ctx->stream);
     }
     c64 = nullptr;
     *out = f;
@@ -289,17 +286,15 @@ qew_status qew_field_create_generated(qew_ctx *ctx, int nx, int ny, double Lx, d
     const std::vector<double> tx = gauss_taps(xi_x_cells, Rx), ty = gauss_taps(xi_y_cells, Ry);
     double *w = nullptr, *t = nullptr, *taps = nullptr;
     auto cleanup = [&](qew_status s) {
-        if (w) cudaFree(w);
-        if (t) cudaFree(t);
-        if (taps) cudaFree(taps);
+        qew_free_async(w, ctx->stream);
+        qew_free_async(t, ctx->stream);
+        qew_free_async(taps, ctx->stream);
         return s;
     };
-    if (cudaMalloc(&w, N * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&t, N * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&taps, (tx.size() + ty.size() + 1) * sizeof(double)) != cudaSuccess) {
-        cudaGetLastError();
-        return cleanup(qew_fail(ctx, QEW_ERR_NOMEM, "field_create_generated: cudaMalloc"));
-    }
+    if (qew_alloc_async(ctx, (void **)&w, N * sizeof(double)) != QEW_OK ||
+        qew_alloc_async(ctx, (void **)&t, N * sizeof(double)) != QEW_OK ||
+        qew_alloc_async(ctx, (void **)&taps, (tx.size() + ty.size() + 1) * sizeof(double)) != QEW_OK)
+        return cleanup(QEW_ERR_NOMEM);
     double *tapx = taps, *tapy = taps + tx.size(), *scale = tapy + ty.size();
     cudaError_t e = cudaMemcpyAsync(tapx, tx.data(), tx.size() * sizeof(double),
                                     cudaMemcpyHostToDevice, ctx->stream);
@@ -338,11 +333,22 @@ qew_status qew_field_create_analytic(qew_ctx *ctx, int kind, double p0, double p
 qew_status qew_field_destroy(qew_field *f) {
     if (!f) return QEW_OK;
     cudaSetDevice(f->device);
+    // the coefficients may be in use on any stream: wait for the device
     if (f->coef64 || f->coef32) cudaDeviceSynchronize();
-    if (f->coef64) cudaFree(f->coef64);
-    if (f->coef32) cudaFree(f->coef32);
+    qew_free_async(f->coef64, f->stream);
+    qew_free_async(f->coef32, f->stream);
+    if (f->coef64 || f->coef32) cudaStreamSynchronize(f->stream);
     delete f;
     return QEW_OK;
+}
+
+// Release a field whose coefficients were only used on `stream`: frees in
+// that stream's order, without waiting for the rest of the device.
+void qew_field_release_on(qew_field *f, cudaStream_t stream) {
+    if (!f) return;
+    qew_free_async(f->coef64, stream);
+    qew_free_async(f->coef32, stream);
+    delete f;
 }
 
 qew_status qew_field_get_coefficients(qew_ctx *ctx, const qew_field *f, double *h_coef) {

@@ -45,12 +45,16 @@ struct qew_field {
     double p0 = 0, p1 = 0, p2 = 0;
     double *coef64 = nullptr;  // [ny][nx], x fastest
     float *coef32 = nullptr;   // [ny][nx], x fastest
+    cudaStream_t stream = nullptr;  // stream the coefficients were allocated on
 };
 
 #define QEW_RED_MAX_BLOCKS 1024
 
 // Records the message on ctx (if any) and returns the status.
 qew_status qew_fail(qew_ctx *ctx, qew_status s, const char *fmt, ...);
+// Stream-ordered device allocation on ctx's stream (no device-wide sync).
+qew_status qew_alloc_async(qew_ctx *ctx, void **p, size_t bytes);
+void qew_free_async(void *p, cudaStream_t stream);
 // Ensures ctx->scratch holds at least `bytes` (256-byte aligned base).
 qew_status qew_scratch_reserve(qew_ctx *ctx, size_t bytes);
 // Checks the last launch; bumps the launch counter by `k`.

@@ -164,10 +164,9 @@ qew_status qew_langevin_create(qew_ctx *ctx, int n, uint64_t seed, qew_langevin 
     l->ctx = ctx;
     l->n = n;
     l->seed = seed;
-    if (cudaMalloc(&l->grad, sizeof(double) * (size_t)n) != cudaSuccess) {
-        cudaGetLastError();
+    if (qew_alloc_async(ctx, (void **)&l->grad, sizeof(double) * (size_t)n) != QEW_OK) {
         delete l;
-        return qew_fail(ctx, QEW_ERR_NOMEM, "langevin_create: cudaMalloc");
+        return QEW_ERR_NOMEM;
     }
     *out = l;
     return QEW_OK;
@@ -175,10 +174,7 @@ qew_status qew_langevin_create(qew_ctx *ctx, int n, uint64_t seed, qew_langevin 
 
 qew_status qew_langevin_destroy(qew_langevin *l) {
     if (!l) return QEW_OK;
-    if (l->grad) {
-        cudaStreamSynchronize(l->ctx->stream);
-        cudaFree(l->grad);
-    }
+    if (l->grad) qew_free_async(l->grad, l->ctx->stream);
     delete l;
     return QEW_OK;
 }

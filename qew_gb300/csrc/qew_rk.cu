@@ -163,10 +163,7 @@ qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, doubl
         return qew_fail(ctx, QEW_ERR_INVALID, "depinning_bisect: bad arguments");
     QEW_TRY(qew_rk_validate(ctx, n, p, rp));
     double *work = nullptr;
-    if (cudaMalloc(&work, sizeof(double) * (size_t)n) != cudaSuccess) {
-        cudaGetLastError();
-        return qew_fail(ctx, QEW_ERR_NOMEM, "depinning_bisect: cudaMalloc");
-    }
+    QEW_TRY(qew_alloc_async(ctx, (void **)&work, sizeof(double) * (size_t)n));
     qew_params pp = *p;
     int steps = 0;
     qew_status st = QEW_OK;
@@ -197,8 +194,8 @@ qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, doubl
             f_hi = fm;
         }
     }
+    qew_free_async(work, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
-    cudaFree(work);
     if (st != QEW_OK) return st;
     *f_c = 0.5 * (f_lo + f_hi);
     if (f_lo_out) *f_lo_out = f_lo;

@@ -22,7 +22,7 @@
 
 namespace {
 
-constexpr int kRkBS = 128;
+constexpr int kRkBS = 32;  // one warp per CTA: a 16384-site line still spreads over every SM
 template <class Noise>
 __global__ void __launch_bounds__(kRkBS)
 k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n, double dx,

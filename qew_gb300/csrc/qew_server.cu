@@ -1,0 +1,317 @@
+// qew_server.cu -- serving: continuous batching of mixed requests (static
+// minimisation, annealed Langevin, depinning f_c) with admission by an HBM
+// budget. No reference counterpart: the reference runs one simulation per
+// process (the three executables).
+//
+// Requests enter a FIFO queue. Each of `max_inflight` workers owns a context
+// on its own non-blocking CUDA stream; a worker admits the queue head as soon
+// as the head's device-memory estimate fits in the budget left by the
+// requests in flight, so requests arriving while others run are admitted as
+// slots and memory free up and their kernels overlap on the device. Every
+// buffer of a request (its generated field, its line, its solver state)
+// lives on the device and is allocated and released in its stream's order,
+// so finishing one request never waits for the others. Every kernel involved
+// is deterministic with a launch shape fixed by the request alone, so a
+// request's result is the same whether it runs alone or in the mix.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "qew_internal.cuh"
+#include "qew_rk_internal.cuh"
+#include "qew_vec.cuh"
+
+extern "C" void qew_field_release_on(qew_field *f, cudaStream_t stream);
+
+struct qew_server {
+    int device = 0;
+    double budget = 0;
+    double used = 0;
+    int max_inflight = 1;
+    std::mutex mu;
+    std::condition_variable cv;
+    struct Job {
+        uint64_t id;
+        qew_request req;
+        double t_submit;
+        double est;
+    };
+    std::deque<Job> queue;
+    std::vector<qew_response> done;
+    std::vector<std::thread> workers;
+    int running = 0;
+    bool stop = false;
+    uint64_t next_id = 1;
+    std::chrono::steady_clock::time_point t0;
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+// Device bytes a request holds at its peak: field generation (two FP64
+// work arrays + FP64 and FP32 coefficients) plus line and solver state.
+double request_bytes(const qew_request &r) {
+    const double cells = (double)r.n * (double)r.rows;
+    return cells * (8.0 * 2 + 8.0 + 4.0) + (double)r.n * 8.0 * 40.0 + (1 << 20);
+}
+
+qew_status run_static(qew_ctx *ctx, const qew_request &r, qew_field *f, double *h,
+                      qew_response &out) {
+    QEW_CUDA(ctx, cudaMemsetAsync(h, 0, sizeof(double) * (size_t)r.n, ctx->stream));
+    qew_ensemble_line line;
+    line.field = f;
+    line.d_h = h;
+    line.n = r.n;
+    line.p = qew_params{(double)r.n, r.line_tension, r.driving_force, r.model};
+    line.precond_shift = 0.5 / (r.xi * r.xi);  // 0.5 dx A / xi^2 (qew_runs.h:89-91), dx = A = 1
+    qew_ensemble_params ep;
+    qew_lbfgs_default_params(&ep.lbfgs);
+    ep.lbfgs.m = 10;
+    ep.lbfgs.ftol = r.ftol;
+    ep.lbfgs.max_iter = 20000;
+    ep.lbfgs.precondition = 1;
+    ep.lbfgs.ls_fallback = 1;
+    ep.ftol_fp32 = 2e-5;
+    ep.max_iter_fp32 = 0;
+    qew_lbfgs_result res;
+    QEW_TRY(qew_ensemble_minimize(ctx, 1, &line, &ep, &res));
+    out.iterations = res.iterations;
+    out.max_force = res.max_force;
+    out.converged = res.converged;
+    return qew_objective(ctx, f, h, r.n, &line.p, &out.value);
+}
+
+qew_status run_langevin(qew_ctx *ctx, const qew_request &r, qew_field *f, double *h,
+                        qew_response &out) {
+    std::vector<double> hv((size_t)r.n, 0.5 * r.rows);
+    QEW_CUDA(ctx, cudaMemcpyAsync(h, hv.data(), sizeof(double) * hv.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    qew_langevin *lgv = nullptr;
+    QEW_TRY(qew_langevin_create(ctx, r.n, r.seed + 1, &lgv));
+    std::vector<double> drift((size_t)r.steps, r.dt), diff((size_t)r.steps,
+                                                         std::sqrt(2.0 * r.temperature * r.dt));
+    const qew_params p{(double)r.n, r.line_tension, r.driving_force, r.model};
+    qew_status st = qew_langevin_run(lgv, f, h, &p, r.steps, drift.data(), diff.data(),
+                                     QEW_PREC_FP32_SPLIT);
+    qew_langevin_destroy(lgv);
+    QEW_TRY(st);
+    double sum;
+    QEW_TRY((vec_reduce<SumF, 1, false>(ctx, r.n, SumF{h}, &sum)));
+    out.value = sum / r.n;
+    out.iterations = r.steps;
+    out.converged = 1;
+    return QEW_OK;
+}
+
+qew_status run_depinning(qew_ctx *ctx, const qew_request &r, qew_field *f, double *h,
+                         qew_response &out) {
+    if (r.n % 2) return qew_fail(ctx, QEW_ERR_ODD_LENGTH, "depinning request: odd n");
+    std::vector<double> hv((size_t)r.n, 0.5 * r.rows);
+    QEW_CUDA(ctx, cudaMemcpyAsync(h, hv.data(), sizeof(double) * hv.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    // CLI defaults of qew_depinning (main.cpp:75-81) in cells: dstep 1/2,
+    // max_advance Ly, runaway 2 Ly, unless the request caps them
+    qew_rk_params rp{0.5, r.max_advance > 0 ? r.max_advance : (double)r.rows, 1e-10, 1e-8,
+                     r.runaway > 0 ? r.runaway : 2.0 * r.rows, r.max_sweeps};
+    qew_params p{(double)r.n, r.line_tension, 0.0, QEW_MODEL_LINEAR};
+    double *hlo = nullptr;
+    QEW_TRY(qew_alloc_async(ctx, (void **)&hlo, sizeof(double) * (size_t)r.n));
+    double f_lo = -1, f_hi = -1;
+    int blocks = 0;
+    qew_status st = QEW_OK;
+    for (int k = 0; (double)k * r.f_step <= r.f_max; ++k) {  // ramp, qew_runs.h:224-241
+        p.driving_force = (double)k * r.f_step;
+        qew_rk_result rr;
+        st = qew_rk_block_resident(ctx, f, h, r.n, &p, &rp, QEW_PREC_FP32_SPLIT, &rr);
+        ++blocks;
+        if (st != QEW_OK) break;
+        if (!rr.blocked) {
+            f_hi = p.driving_force;
+            break;
+        }
+        f_lo = p.driving_force;
+        cudaMemcpyAsync(hlo, h, sizeof(double) * (size_t)r.n, cudaMemcpyDeviceToDevice, ctx->stream);
+    }
+    if (st == QEW_OK && f_lo >= 0 && f_hi >= 0) {
+        double fc, a, b;
+        int nb = 0;
+        st = qew_depinning_bisect_prec(ctx, f, hlo, r.n, &p, &rp, f_lo, f_hi, r.bisect_rtol, 64,
+                                       QEW_PREC_FP32_SPLIT, &fc, &a, &b, &nb);
+        blocks += nb;
+        out.value = fc;
+        out.converged = 1;
+        cudaMemcpyAsync(h, hlo, sizeof(double) * (size_t)r.n, cudaMemcpyDeviceToDevice, ctx->stream);
+    } else {
+        out.value = f_hi;  // -1: no bracket within f_max
+        out.converged = 0;
+    }
+    out.iterations = blocks;
+    qew_free_async(hlo, ctx->stream);
+    return st;
+}
+
+void worker_main(qew_server *s) {
+    cudaSetDevice(s->device);
+    qew_ctx *ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    const bool ok = qew_ctx_create(s->device, &ctx) == QEW_OK &&
+                    cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) == cudaSuccess;
+    if (ok) qew_ctx_set_stream(ctx, stream);
+    for (;;) {
+        qew_server::Job job;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv.wait(lk, [&] {
+                return s->stop || (!s->queue.empty() &&
+                                   (s->used + s->queue.front().est <= s->budget || s->used == 0));
+            });
+            if (s->stop && s->queue.empty()) break;
+            if (s->stop && !(s->used + s->queue.front().est <= s->budget || s->used == 0)) break;
+            job = s->queue.front();
+            s->queue.pop_front();
+            s->used += job.est;
+            ++s->running;
+        }
+        qew_response out{};
+        out.id = job.id;
+        out.kind = job.req.kind;
+        out.t_submit = job.t_submit;
+        out.t_start = s->now();
+        qew_status st = ok ? QEW_OK : QEW_ERR_CUDA;
+        qew_field *f = nullptr;
+        double *h = nullptr;
+        const qew_request &r = job.req;
+        if (st == QEW_OK) {
+            const int store = (r.kind == QEW_REQ_STATIC) ? (QEW_STORE_FP64 | QEW_STORE_FP32)
+                                                         : QEW_STORE_FP32;
+            st = qew_field_create_generated(ctx, r.n, r.rows, (double)r.n, (double)r.rows, 1.0,
+                                            r.xi, r.xi, r.seed, store, &f);
+        }
+        if (st == QEW_OK) st = qew_alloc_async(ctx, (void **)&h, sizeof(double) * (size_t)r.n);
+        if (st == QEW_OK) {
+            if (r.kind == QEW_REQ_STATIC)
+                st = run_static(ctx, r, f, h, out);
+            else if (r.kind == QEW_REQ_LANGEVIN)
+                st = run_langevin(ctx, r, f, h, out);
+            else if (r.kind == QEW_REQ_DEPINNING)
+                st = run_depinning(ctx, r, f, h, out);
+            else
+                st = QEW_ERR_INVALID;
+        }
+        if (st == QEW_OK && r.h_out)
+            if (cudaMemcpyAsync(r.h_out, h, sizeof(double) * (size_t)r.n, cudaMemcpyDeviceToHost,
+                                stream) != cudaSuccess)
+                st = QEW_ERR_CUDA;
+        if (ctx) {
+            qew_free_async(h, stream);
+            qew_field_release_on(f, stream);
+            if (cudaStreamSynchronize(stream) != cudaSuccess && st == QEW_OK) st = QEW_ERR_CUDA;
+        }
+        out.status = st;
+        out.t_end = s->now();
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->used -= job.est;
+            --s->running;
+            s->done.push_back(out);
+        }
+        s->cv.notify_all();
+    }
+    if (ctx) qew_ctx_destroy(ctx);
+    if (stream) cudaStreamDestroy(stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+qew_status qew_server_create(int device, double hbm_budget_bytes, int max_inflight,
+                             qew_server **out) {
+    if (!out || max_inflight < 1 || max_inflight > 1024 || !(hbm_budget_bytes > 0))
+        return QEW_ERR_INVALID;
+    qew_server *s = new (std::nothrow) qew_server();
+    if (!s) return QEW_ERR_NOMEM;
+    s->device = device;
+    s->budget = hbm_budget_bytes;
+    s->max_inflight = max_inflight;
+    s->t0 = std::chrono::steady_clock::now();
+    try {
+        for (int k = 0; k < max_inflight; ++k) s->workers.emplace_back(worker_main, s);
+    } catch (...) {
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stop = true;
+        }
+        s->cv.notify_all();
+        for (auto &t : s->workers) t.join();
+        delete s;
+        return QEW_ERR_NOMEM;
+    }
+    *out = s;
+    return QEW_OK;
+}
+
+double qew_server_clock(const qew_server *s) { return s ? s->now() : 0.0; }
+
+qew_status qew_server_submit(qew_server *s, const qew_request *req, uint64_t *id) {
+    if (!s || !req || req->n < 2 || req->rows < 4 || !(req->xi >= 0) ||
+        req->kind < QEW_REQ_STATIC || req->kind > QEW_REQ_DEPINNING)
+        return QEW_ERR_INVALID;
+    if (req->kind == QEW_REQ_LANGEVIN && (req->steps < 0 || !(req->dt > 0) || req->temperature < 0))
+        return QEW_ERR_INVALID;
+    if (req->kind == QEW_REQ_DEPINNING &&
+        (req->n % 2 || !(req->f_step > 0) || req->max_sweeps < 1 || !(req->bisect_rtol > 0)))
+        return QEW_ERR_INVALID;
+    const double est = request_bytes(*req);
+    if (est > s->budget) return QEW_ERR_NOMEM;  // could never be admitted
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->stop) return QEW_ERR_INVALID;
+        qew_server::Job j{s->next_id++, *req, s->now(), est};
+        if (id) *id = j.id;
+        s->queue.push_back(j);
+    }
+    s->cv.notify_all();
+    return QEW_OK;
+}
+
+int qew_server_poll(qew_server *s, qew_response *out, int max) {
+    if (!s || !out || max < 1) return 0;
+    std::lock_guard<std::mutex> lk(s->mu);
+    const int k = std::min<int>(max, (int)s->done.size());
+    std::copy(s->done.begin(), s->done.begin() + k, out);
+    s->done.erase(s->done.begin(), s->done.begin() + k);
+    return k;
+}
+
+qew_status qew_server_drain(qew_server *s, double timeout_s) {
+    if (!s) return QEW_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    const bool ok = s->cv.wait_for(lk, std::chrono::duration<double>(timeout_s), [&] {
+        return s->queue.empty() && s->running == 0;
+    });
+    return ok ? QEW_OK : QEW_ERR_TIMEOUT;
+}
+
+qew_status qew_server_destroy(qew_server *s) {
+    if (!s) return QEW_OK;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->queue.clear();
+        s->stop = true;
+    }
+    s->cv.notify_all();
+    for (auto &t : s->workers) t.join();
+    delete s;
+    return QEW_OK;
+}
+
+}  // extern "C"
