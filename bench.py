@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp32split", choices=["fp64", "fp32split"])
     ap.add_argument("--small", action="store_true",
-                    help="small case for profiling: L=2^20, 64-row field, one instance")
+                    help="small case for profiling: the same batched launch (8 lines of "
+                         "L=2^20) on a 256-row field (3 GB of coefficients)")
     ap.add_argument("--profile-run", action="store_true",
                     help="GPU timed loop only (no e2e, CPU baseline or clock sampling)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -430,7 +431,7 @@ def run_serving(args, Q, torch):
     srv = Q.Server(hbm_budget_bytes=150e9, max_inflight=args.serve_inflight)
     out = {"metric": "serving latency p50/p99 and solves/s", "unit": "s",
            "budget_GB": 150, "inflight": args.serve_inflight, "rates": [],
-           "mix": "50% static (1e-8), 30% Langevin (%d steps), 20%% depinning f_c"
+           "mix": "50%% static (1e-8), 30%% Langevin (%d steps), 20%% depinning f_c"
                   % args.serve_lsteps}
     try:
         for ri, rate in enumerate(rates):
@@ -506,7 +507,7 @@ def run_ours(args):
     import qew_gb300 as Q
 
     if args.small:
-        L, ny, n_inst = L_FULL, 64, 1
+        L, ny, n_inst = L_FULL, 256, N_INST
     else:
         L, ny, n_inst = L_FULL, NY_FULL, N_INST
     field = gaussian_field_gpu(torch, L, ny, XI, SEED + rank)

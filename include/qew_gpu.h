@@ -174,6 +174,19 @@ qew_status qew_field_create_generated(qew_ctx *ctx, int nx, int ny, double Lx,
                                       double xi_x_cells, double xi_y_cells,
                                       uint64_t seed, int store_flags,
                                       qew_field **out);
+/* FilteredNoise(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed), the reference's
+ * seeded constructor (filtered_noise.h:183-185, filtered_noise.cpp:25-82):
+ * unit-modulus random phases from std::mt19937_64(seed) through
+ * std::uniform_real_distribution(0, 2 pi), drawn in the reference's order and
+ * zeroed outside the correlation ellipse (fx xi_x)^2 + (fy xi_y)^2 <= 1, an
+ * inverse FFT2 with 1/(nx ny) normalisation (cuFFT on the device), the real
+ * part scaled to population std `amplitude` (mean kept), then prefiltered as
+ * qew_field_create_from_host. The phases are drawn on the host (the
+ * generator is sequential); everything after runs on the device. */
+qew_status qew_field_create_seeded(qew_ctx *ctx, int nx, int ny, double Lx,
+                                   double Ly, double amplitude, double xi_x,
+                                   double xi_y, uint64_t seed, int store_flags,
+                                   qew_field **out);
 /* Analytic potentials (see the kind enum). */
 qew_status qew_field_create_analytic(qew_ctx *ctx, int kind, double p0,
                                      double p1, double p2, qew_field **out);

@@ -92,6 +92,11 @@ def lib():
                                           PD, PD, PD, C.POINTER(I)]
         L.qo_depinning_bisect.restype = I
         L.qo_philox_normals.argtypes = [C.c_uint64, C.c_uint64, I, PD]
+        L.qo_mt64_seed.argtypes = [C.c_void_p, C.c_uint64]
+        L.qo_mt64_next.argtypes = [C.c_void_p]
+        L.qo_mt64_next.restype = C.c_uint64
+        L.qo_seeded_field.argtypes = [I, I, D, D, D, D, D, C.c_uint64, PD]
+        L.qo_seeded_field.restype = I
     return _lib
 
 
@@ -269,3 +274,18 @@ def fft(re, im, inverse=False):
     im = np.array(im, dtype=np.float64)
     lib().qo_fft(_p(re), _p(im), re.size, 1 if inverse else 0)
     return re, im
+
+
+def mt64_outputs(seed: int, count: int) -> np.ndarray:
+    """The first `count` outputs of std::mt19937_64(seed), restated."""
+    st = C.create_string_buffer(312 * 8 + 16)
+    lib().qo_mt64_seed(st, seed)
+    return np.array([lib().qo_mt64_next(st) for _ in range(count)], dtype=np.uint64)
+
+
+def seeded_field(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed) -> np.ndarray:
+    """FilteredNoise's seeded field (filtered_noise.cpp:25-82), [nx][ny]."""
+    out = np.empty((nx, ny))
+    if lib().qo_seeded_field(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed, _p(out)) != 0:
+        raise MemoryError("qo_seeded_field")
+    return out

@@ -338,6 +338,109 @@ int qo_prefilter(const double *field, int nx, int ny, double *coef) {
 }
 
 /* ======================================================================== */
+/* Seeded field (FilteredNoise's generating constructor)                    */
+/* ======================================================================== */
+
+/* The 64-bit Mersenne Twister with the parameters of C++'s std::mt19937_64
+ * (Matsumoto and Nishimura, ACM TOMACS 8 (1998); Nishimura, ACM TOMACS 10
+ * (2000)): w = 64, n = 312, m = 156, r = 31, a = 0xb5026f5aa96619e9,
+ * (u, d) = (29, 0x5555555555555555), (s, b) = (17, 0x71d67fffeda60000),
+ * (t, c) = (37, 0xfff7eee000000000), l = 43, seeding multiplier
+ * 6364136223846793005. */
+void qo_mt64_seed(qo_mt64 *g, uint64_t seed) {
+    g->mt[0] = seed;
+    for (int i = 1; i < 312; ++i)
+        g->mt[i] = 6364136223846793005ULL * (g->mt[i - 1] ^ (g->mt[i - 1] >> 62)) + (uint64_t)i;
+    g->idx = 312;
+}
+
+uint64_t qo_mt64_next(qo_mt64 *g) {
+    const uint64_t upper = ~0ULL << 31, lower = (1ULL << 31) - 1;
+    if (g->idx >= 312) {
+        for (int i = 0; i < 312; ++i) {
+            const uint64_t x = (g->mt[i] & upper) | (g->mt[(i + 1) % 312] & lower);
+            uint64_t xa = x >> 1;
+            if (x & 1) xa ^= 0xb5026f5aa96619e9ULL;
+            g->mt[i] = g->mt[(i + 156) % 312] ^ xa;
+        }
+        g->idx = 0;
+    }
+    uint64_t y = g->mt[g->idx++];
+    y ^= (y >> 29) & 0x5555555555555555ULL;
+    y ^= (y << 17) & 0x71d67fffeda60000ULL;
+    y ^= (y << 37) & 0xfff7eee000000000ULL;
+    y ^= y >> 43;
+    return y;
+}
+
+/* std::uniform_real_distribution<double>(a, b) over a 64-bit engine as
+ * libstdc++ evaluates it: generate_canonical<double, 53> takes one draw,
+ * u = double(x) / 2^64 (nudged below 1 if it rounds up to 1), then
+ * u * (b - a) + a. */
+double qo_mt64_uniform(qo_mt64 *g, double a, double b) {
+    double u = (double)qo_mt64_next(g) / 18446744073709551616.0;
+    if (u >= 1.0) u = nextafter(1.0, 0.0);
+    return u * (b - a) + a;
+}
+
+static double qo_fftfreq(int k, int n) { /* filtered_noise.cpp:18-21 */
+    const int ks = (k < (n + 1) / 2) ? k : k - n;
+    return (double)ks / (double)n;
+}
+
+/* FilteredNoise(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed),
+ * filtered_noise.cpp:25-82: masked random phases, inverse FFT2 (1/(nx ny)),
+ * real part scaled to population std `amplitude`. field is [nx][ny]. */
+int qo_seeded_field(int nx, int ny, double Lx, double Ly, double amplitude, double xi_x,
+                    double xi_y, uint64_t seed, double *field) {
+    const size_t N = (size_t)nx * ny;
+    double *re = (double *)malloc(sizeof(double) * 2 * N);
+    const int nl = nx > ny ? nx : ny;
+    double *lre = (double *)malloc(sizeof(double) * 2 * (size_t)nl);
+    qo_mt64 *g = (qo_mt64 *)malloc(sizeof(qo_mt64));
+    if (!re || !lre || !g) { free(re); free(lre); free(g); return -1; }
+    double *im = re + N, *lim = lre + nl;
+    const double two_pi = 2.0 * acos(-1.0);
+    const double dx = Lx / nx, dy = Ly / ny;
+    qo_mt64_seed(g, seed);
+    for (int i = 0; i < nx; ++i) {
+        const double fx = qo_fftfreq(i, nx) / dx;
+        for (int j = 0; j < ny; ++j) {
+            const double fy = qo_fftfreq(j, ny) / dy;
+            const double ph = qo_mt64_uniform(g, 0.0, two_pi);
+            const size_t k = (size_t)i * ny + j;
+            if ((fx * xi_x) * (fx * xi_x) + (fy * xi_y) * (fy * xi_y) > 1.0) {
+                re[k] = 0.0;
+                im[k] = 0.0;
+            } else {
+                re[k] = cos(ph);
+                im[k] = sin(ph);
+            }
+        }
+    }
+    for (int i = 0; i < nx; ++i) qo_fft(re + (size_t)i * ny, im + (size_t)i * ny, ny, 1);
+    for (int j = 0; j < ny; ++j) {
+        for (int i = 0; i < nx; ++i) { lre[i] = re[(size_t)i * ny + j]; lim[i] = im[(size_t)i * ny + j]; }
+        qo_fft(lre, lim, nx, 1);
+        for (int i = 0; i < nx; ++i) re[(size_t)i * ny + j] = lre[i];
+    }
+    double mean = 0.0;
+    for (size_t k = 0; k < N; ++k) mean += re[k];
+    mean /= (double)N;
+    double var = 0.0;
+    for (size_t k = 0; k < N; ++k) {
+        const double d = re[k] - mean;
+        var += d * d;
+    }
+    const double scale = amplitude / sqrt(var / (double)N);
+    for (size_t k = 0; k < N; ++k) field[k] = re[k] * scale;
+    free(re);
+    free(lre);
+    free(g);
+    return 0;
+}
+
+/* ======================================================================== */
 /* Model: objective and gradient (qew_model.h)                              */
 /* ======================================================================== */
 

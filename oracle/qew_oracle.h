@@ -95,6 +95,14 @@ void qo_sample_many(const qo_noise *nz, const double *x, const double *y, int m,
 /* Prefilter field (row-major i*ny+j) -> coef (same layout). */
 int qo_prefilter(const double *field, int nx, int ny, double *coef);
 
+/* ---- std::mt19937_64 and the seeded field (filtered_noise.cpp:25-82) ---- */
+typedef struct { uint64_t mt[312]; int idx; } qo_mt64;
+void qo_mt64_seed(qo_mt64 *g, uint64_t seed);
+uint64_t qo_mt64_next(qo_mt64 *g);
+double qo_mt64_uniform(qo_mt64 *g, double a, double b);
+int qo_seeded_field(int nx, int ny, double Lx, double Ly, double amplitude, double xi_x,
+                    double xi_y, uint64_t seed, double *field);
+
 /* ---- complex / real FFT (kokkos-fft semantics: forward unnormalised,
  * backward 1/n) ---- */
 int qo_fft(double *re, double *im, int n, int inverse);

@@ -19,6 +19,8 @@ test stubs (ZeroNoise, HarmonicWell, ...)  :func:`ZeroNoise` etc.
 ``lbfgs_minimize(h, p, noise, lp)``        :func:`lbfgs_minimize`
 ``LangevinDynamics(n, seed).step(...)``    :class:`LangevinDynamics`
 ``rk_site_velocity`` / ``rk_block``        :func:`rk_site_velocity`, :func:`rk_block`
+``static_sweep`` / ``dynamic_anneal`` /    :func:`static_sweep`, :func:`dynamic_anneal`,
+``depinning_ramp`` (qew_runs.h)            :func:`depinning_ramp`
 =========================================  ====================================
 
 ``rk_block`` raises ``ValueError`` on an odd line length where the reference
@@ -47,6 +49,9 @@ __all__ = [
     "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
     "depinning_bisect", "Context", "default_context", "QewError", "Server",
+    "StaticConfig", "StaticProfile", "static_sweep", "DynamicConfig", "DynamicSnapshot",
+    "DynamicResult", "dynamic_anneal", "DepinningConfig", "DepinningStep", "DepinningResult",
+    "depinning_ramp",
 ]
 
 
@@ -246,6 +251,26 @@ class FilteredNoise(_Noise):
             self.ctx.h, int(nx), int(ny), float(Lx), float(Ly), float(amplitude),
             float(xi_x_cells), float(xi_y_cells), int(seed), int(store), C.byref(h)),
             self.ctx.h, "FilteredNoise.generated")
+        self.h = h
+        self.nx, self.ny, self.Lx, self.Ly = int(nx), int(ny), float(Lx), float(Ly)
+        self.dx, self.dy = self.Lx / nx, self.Ly / ny
+        self.store = store
+        return self
+
+    @classmethod
+    def seeded(cls, nx: int, ny: int, Lx: float, Ly: float, amplitude: float, xi_x: float,
+               xi_y: float, seed: int, store: int = QEW_STORE_FP64,
+               ctx: Context | None = None) -> "FilteredNoise":
+        """FilteredNoise(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed): the
+        reference's seeded constructor (filtered_noise.cpp:25-82)."""
+        self = cls.__new__(cls)
+        _Noise.__init__(self)
+        self.ctx = ctx or default_context()
+        h = C.c_void_p()
+        _capi.check(self.ctx.lib.qew_field_create_seeded(
+            self.ctx.h, int(nx), int(ny), float(Lx), float(Ly), float(amplitude),
+            float(xi_x), float(xi_y), int(seed), int(store), C.byref(h)),
+            self.ctx.h, "FilteredNoise.seeded")
         self.h = h
         self.nx, self.ny, self.Lx, self.Ly = int(nx), int(ny), float(Lx), float(Ly)
         self.dx, self.dy = self.Lx / nx, self.Ly / ny
@@ -588,6 +613,175 @@ def depinning_bisect(h, p: Params, noise: _Noise, rp: RkParams, f_lo: float, f_h
         float(rtol), int(max_steps), int(precision), C.byref(fc), C.byref(flo), C.byref(fhi),
         C.byref(nb)), ctx.h, "depinning_bisect")
     return fc.value, flo.value, fhi.value, nb.value
+
+
+# ---------------------------------------------------------------- drivers
+# static_sweep / dynamic_anneal / depinning_ramp, qew_runs.h:45-243 (same
+# configuration fields and defaults; the additive knobs are marked).
+def _lbfgs_result(r) -> LbfgsResult:
+    return LbfgsResult(r.iterations, r.max_force, bool(r.converged), r.n_func_evals,
+                       r.n_curvature_skips, r.n_ls_restarts)
+
+
+def _rk_result(r) -> RkResult:
+    return RkResult(bool(r.blocked), bool(r.runaway), r.sweeps, r.total_advance, r.mean_h)
+
+
+@dataclass
+class StaticConfig:  # qew_runs.h:48-61
+    model: Model = Model.Arclength
+    amplitude: float = 1.0
+    xi: float = 0.1
+    Lx: float = 32.0
+    Ly: float = 1.0
+    nx: int = 4096
+    ny: int = 512
+    driving_force: float = 0.0
+    pinning_lengths_over_xi: tuple = (0.01, 0.1, 1.0, 10.0, 100.0)
+    ftol: float = 1e-6
+    max_iter: int = 5000
+    lbfgs_m: int = 8  # additive
+
+
+@dataclass
+class StaticProfile:  # qew_runs.h:63-68
+    pinning_length_over_xi: float
+    line_tension: float
+    h: np.ndarray
+    result: LbfgsResult
+
+
+def static_sweep(c: StaticConfig, noise: _Noise) -> list[StaticProfile]:
+    """static_sweep(c, noise), qew_runs.h:70-102 (one persistent launch for all
+    ratios on a B-spline field)."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    ratios = np.ascontiguousarray(c.pinning_lengths_over_xi, dtype=np.float64)
+    K = len(ratios)
+    cc = _capi.qew_static_config(int(c.model), float(c.amplitude), float(c.xi), float(c.Lx),
+                                 float(c.Ly), int(c.nx), int(c.ny), float(c.driving_force),
+                                 ratios.ctypes.data_as(_capi.PD), K, float(c.ftol),
+                                 int(c.max_iter), int(c.lbfgs_m))
+    prof = (_capi.qew_static_profile * max(K, 1))()
+    h = np.empty((K, int(c.nx)))
+    _capi.check(ctx.lib.qew_static_sweep(ctx.h, noise.h, C.byref(cc), prof,
+                                         h.ctypes.data_as(_capi.PD)), ctx.h, "static_sweep")
+    return [StaticProfile(prof[k].pinning_length_over_xi, prof[k].line_tension, h[k].copy(),
+                          _lbfgs_result(prof[k].result)) for k in range(K)]
+
+
+@dataclass
+class DynamicConfig:  # qew_runs.h:107-122
+    model: Model = Model.Arclength
+    amplitude: float = 1.0
+    xi: float = 0.1
+    pinning_length_over_xi: float = 0.1
+    driving_force: float = 0.0
+    Lx: float = 2.0
+    Ly: float = 1.0
+    nx: int = 2048
+    ny: int = 1024
+    seed: int = 1
+    tau: float = 1.0
+    tl_start: float = 0.01
+    tl_end: float = 0.0001
+    total_time: float = 1000.0
+    dt: float = 0.0  # additive: > 0 replaces the timestep heuristic
+    precision: int = QEW_PREC_FP64  # additive
+
+
+@dataclass
+class DynamicSnapshot:  # qew_runs.h:124-127
+    t: float
+    h: np.ndarray
+
+
+@dataclass
+class DynamicResult:  # qew_runs.h:129-134
+    dt: float
+    total_time: float
+    line_tension: float
+    snapshots: list
+    steps: int = 0
+
+
+def dynamic_anneal(c: DynamicConfig, noise: _Noise) -> DynamicResult:
+    """dynamic_anneal(c, noise), qew_runs.h:136-177."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    cc = _capi.qew_dynamic_config(int(c.model), float(c.amplitude), float(c.xi),
+                                  float(c.pinning_length_over_xi), float(c.driving_force),
+                                  float(c.Lx), float(c.Ly), int(c.nx), int(c.ny), int(c.seed),
+                                  float(c.tau), float(c.tl_start), float(c.tl_end),
+                                  float(c.total_time), float(c.dt), int(c.precision))
+    snaps = []
+
+    def on(user, t, h, n):
+        snaps.append(DynamicSnapshot(t, np.ctypeslib.as_array(h, shape=(n,)).copy()))
+
+    cb = _capi.SNAPSHOT_FN(on)
+    r = _capi.qew_dynamic_result()
+    _capi.check(ctx.lib.qew_dynamic_anneal(ctx.h, noise.h, C.byref(cc), cb, None, C.byref(r)),
+                ctx.h, "dynamic_anneal")
+    return DynamicResult(r.dt, r.total_time, r.line_tension, snaps, r.steps)
+
+
+@dataclass
+class DepinningConfig:  # qew_runs.h:182-194
+    model: Model = Model.Arclength
+    amplitude: float = 1.0
+    xi: float = 0.1
+    pinning_length_over_xi: float = 5.0
+    Lx: float = 8.0
+    Ly: float = 1.0
+    nx: int = 1024
+    ny: int = 256
+    f_step: float = 1.0
+    f_max: float = 40.0
+    rp: RkParams = None  # the caller fills it, as the reference's
+    bisect_rtol: float = 0.0  # additive: > 0 bisects f_c after the ramp
+    precision: int = QEW_PREC_FP64  # additive
+
+
+@dataclass
+class DepinningStep:  # qew_runs.h:196-200
+    f: float
+    result: RkResult
+    h: np.ndarray | None  # blocked steps only
+
+
+@dataclass
+class DepinningResult:  # qew_runs.h:202-206
+    line_tension: float
+    f_c_upper_bound: float
+    steps: list
+    f_c: float = -1.0  # additive (bisection)
+    f_c_bracket: tuple = (-1.0, -1.0)
+    bisect_blocks: int = 0
+
+
+def depinning_ramp(c: DepinningConfig, noise: _Noise) -> DepinningResult:
+    """depinning_ramp(c, noise), qew_runs.h:208-243; raises ValueError on odd nx."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    rp = c.rp if c.rp is not None else RkParams()
+    cc = _capi.qew_depinning_config(int(c.model), float(c.amplitude), float(c.xi),
+                                    float(c.pinning_length_over_xi), float(c.Lx), float(c.Ly),
+                                    int(c.nx), int(c.ny), float(c.f_step), float(c.f_max),
+                                    rp.c(), float(c.bisect_rtol), int(c.precision))
+    steps = []
+
+    def on(user, st, h, n):
+        s = st.contents
+        steps.append(DepinningStep(s.f, _rk_result(s.result),
+                                   np.ctypeslib.as_array(h, shape=(n,)).copy() if h else None))
+
+    cb = _capi.DEPINNING_FN(on)
+    r = _capi.qew_depinning_result()
+    _capi.check(ctx.lib.qew_depinning_ramp(ctx.h, noise.h, C.byref(cc), cb, None, C.byref(r)),
+                ctx.h, "depinning_ramp")
+    return DepinningResult(r.line_tension, r.f_c_upper_bound, steps, r.f_c,
+                           (r.f_c_lo, r.f_c_hi), r.bisect_blocks)
 
 
 # ---------------------------------------------------------------- serving

@@ -12,6 +12,7 @@ import re
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libqew_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "qew_gpu.h")
+HEADERS = [HEADER, os.path.join(os.path.dirname(HERE), "include", "qew_runs.h")]
 
 D, I, U64, VP = C.c_double, C.c_int, C.c_uint64, C.c_void_p
 PD = C.POINTER(C.c_double)
@@ -82,6 +83,47 @@ class qew_response(C.Structure):
                 ("converged", I)]
 
 
+class qew_static_config(C.Structure):
+    _fields_ = [("model", I), ("amplitude", D), ("xi", D), ("Lx", D), ("Ly", D), ("nx", I),
+                ("ny", I), ("driving_force", D), ("pinning_lengths_over_xi", PD),
+                ("n_pinning_lengths", I), ("ftol", D), ("max_iter", I), ("lbfgs_m", I)]
+
+
+class qew_static_profile(C.Structure):
+    _fields_ = [("pinning_length_over_xi", D), ("line_tension", D), ("result", qew_lbfgs_result)]
+
+
+class qew_dynamic_config(C.Structure):
+    _fields_ = [("model", I), ("amplitude", D), ("xi", D), ("pinning_length_over_xi", D),
+                ("driving_force", D), ("Lx", D), ("Ly", D), ("nx", I), ("ny", I), ("seed", U64),
+                ("tau", D), ("tl_start", D), ("tl_end", D), ("total_time", D), ("dt", D),
+                ("precision", I)]
+
+
+class qew_dynamic_result(C.Structure):
+    _fields_ = [("dt", D), ("total_time", D), ("line_tension", D), ("steps", C.c_longlong),
+                ("snapshots", I)]
+
+
+class qew_depinning_config(C.Structure):
+    _fields_ = [("model", I), ("amplitude", D), ("xi", D), ("pinning_length_over_xi", D),
+                ("Lx", D), ("Ly", D), ("nx", I), ("ny", I), ("f_step", D), ("f_max", D),
+                ("rp", qew_rk_params), ("bisect_rtol", D), ("precision", I)]
+
+
+class qew_depinning_step(C.Structure):
+    _fields_ = [("f", D), ("result", qew_rk_result)]
+
+
+class qew_depinning_result(C.Structure):
+    _fields_ = [("line_tension", D), ("f_c_upper_bound", D), ("steps", I), ("f_c", D),
+                ("f_c_lo", D), ("f_c_hi", D), ("bisect_blocks", I)]
+
+
+SNAPSHOT_FN = C.CFUNCTYPE(None, VP, D, PD, I)
+DEPINNING_FN = C.CFUNCTYPE(None, VP, C.POINTER(qew_depinning_step), PD, I)
+
+
 class QewError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__("%s (status %d)" % (msg, status))
@@ -103,6 +145,7 @@ _SIGS = {
     "qew_field_create_from_device": (I, [VP, VP, I, I, D, D, I, C.POINTER(VP)]),
     "qew_field_create_analytic": (I, [VP, I, D, D, D, C.POINTER(VP)]),
     "qew_field_create_generated": (I, [VP, I, I, D, D, D, D, D, U64, I, C.POINTER(VP)]),
+    "qew_field_create_seeded": (I, [VP, I, I, D, D, D, D, D, U64, I, C.POINTER(VP)]),
     "qew_field_destroy": (I, [VP]),
     "qew_field_get_coefficients": (I, [VP, VP, PD]),
     "qew_field_sample": (I, [VP, VP, VP, VP, I, VP, VP, VP]),
@@ -149,12 +192,22 @@ _SIGS = {
     "qew_depinning_bisect_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params),
                                       C.POINTER(qew_rk_params), D, D, D, I, I, PD, PD, PD,
                                       C.POINTER(I)]),
+    # drivers (qew_runs.h)
+    "qew_static_config_default": (None, [C.POINTER(qew_static_config)]),
+    "qew_static_sweep": (I, [VP, VP, C.POINTER(qew_static_config),
+                             C.POINTER(qew_static_profile), PD]),
+    "qew_dynamic_config_default": (None, [C.POINTER(qew_dynamic_config)]),
+    "qew_dynamic_anneal": (I, [VP, VP, C.POINTER(qew_dynamic_config), SNAPSHOT_FN, VP,
+                               C.POINTER(qew_dynamic_result)]),
+    "qew_depinning_config_default": (None, [C.POINTER(qew_depinning_config)]),
+    "qew_depinning_ramp": (I, [VP, VP, C.POINTER(qew_depinning_config), DEPINNING_FN, VP,
+                               C.POINTER(qew_depinning_result)]),
 }
 
 
 def header_symbols() -> list[str]:
-    """Every function the public header declares."""
-    txt = open(HEADER).read()
+    """Every function the public headers declare."""
+    txt = "".join(open(h).read() for h in HEADERS)
     return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(qew_[a-z0-9_]+)\s*\(",
                                  txt, re.M)))
 

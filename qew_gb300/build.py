@@ -2,9 +2,11 @@
 
 Compiles every ``csrc/*.cu`` for sm_103a with nvcc (in parallel, one object
 per translation unit) and links ``_lib/libqew_gb300.so``, which exports the C
-ABI declared in ``include/qew_gpu.h``. cudart is linked statically; cuFFT
-(used only by the host-driven comparator form of L-BFGS) dynamically, with an
-rpath to the toolkit's library directory.
+ABI declared in ``include/qew_gpu.h`` and ``include/qew_runs.h``. cudart is
+linked statically; cuFFT (the host-driven comparator form of L-BFGS and the
+seeded field's inverse transform) dynamically, with an rpath to the toolkit's
+library directory. Then builds the three simulation executables
+(``csrc/cli/*.cpp``, host C++ over that library) into ``_lib/bin``.
 """
 from __future__ import annotations
 
@@ -20,6 +22,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libqew_gb300.so")
+BIN_DIR = os.path.join(OUT_DIR, "bin")
+CLI_DIR = os.path.join(CSRC, "cli")
+EXECUTABLES = ("qew_static", "qew_dynamic", "qew_depinning")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -38,7 +43,37 @@ def _cuda_home() -> str:
 
 
 def _headers():
-    return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    return (glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(INCLUDE, "*.h")) +
+            glob.glob(os.path.join(CLI_DIR, "*.h")))
+
+
+def executable(name: str) -> str:
+    """Path of one of the built simulation executables."""
+    return os.path.join(BIN_DIR, name)
+
+
+def _build_executables(force: bool) -> None:
+    os.makedirs(BIN_DIR, exist_ok=True)
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler for the executables")
+
+    def one(name):
+        src = os.path.join(CLI_DIR, name + ".cpp")
+        out = executable(name)
+        if not force and os.path.exists(out) and not _stale(out, [src, LIB]):
+            return out
+        tmp = out + ".tmp%d" % os.getpid()
+        cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I" + INCLUDE, "-I" + CLI_DIR, src, "-o", tmp,
+               "-L" + OUT_DIR, "-lqew_gb300", "-Wl,-rpath,$ORIGIN/.."]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("g++ failed for %s:\n%s\n%s" % (src, " ".join(cmd), r.stderr))
+        os.replace(tmp, out)
+        return out
+
+    with cf.ThreadPoolExecutor(len(EXECUTABLES)) as ex:
+        list(ex.map(one, EXECUTABLES))
 
 
 def _stale(lib: str, srcs) -> bool:
@@ -51,6 +86,7 @@ def _stale(lib: str, srcs) -> bool:
 def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     if not force and not _stale(LIB, srcs):
+        _build_executables(force)
         return LIB
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
@@ -78,6 +114,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB)
+    _build_executables(True)
     return LIB
 
 

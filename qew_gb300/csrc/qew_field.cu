@@ -12,8 +12,12 @@
 #include "qew_internal.cuh"
 #include "qew_philox.cuh"
 
+#include <cufft.h>
+
+#include <algorithm>
 #include <cmath>
 #include <new>
+#include <random>
 #include <vector>
 
 namespace {
@@ -176,6 +180,21 @@ __global__ void k_std_scale(const double *__restrict__ a, size_t n, double ampli
     if (threadIdx.x == 0) *scale = amplitude / sqrt(s2 / (double)n);
 }
 
+// Real part of the inverse transform times 1/(nx ny) (the backward
+// normalisation of kokkos-fft and numpy's ifft2).
+__global__ void k_real_part(const cufftDoubleComplex *__restrict__ b, size_t n, double inv_n,
+                            double *__restrict__ out) {
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x)
+        out[k] = b[k].x * inv_n;
+}
+
+// numpy fftfreq(n)[k] in cycles per sample (filtered_noise.cpp:18-21).
+double fft_freq(int k, int n) {
+    const int ks = (k < (n + 1) / 2) ? k : k - n;
+    return (double)ks / (double)n;
+}
+
 std::vector<double> gauss_taps(double xi, int &R) {
     R = (xi > 0) ? (int)ceil(5.0 * xi) : 0;
     std::vector<double> t(2 * R + 1);
@@ -313,6 +332,83 @@ qew_status qew_field_create_generated(qew_ctx *ctx, int nx, int ny, double Lx, d
     if (st != QEW_OK) return cleanup(st);
     st = field_build(ctx, w, true, nx, ny, Lx, Ly, store_flags, out);
     return cleanup(st);
+}
+
+qew_status qew_field_create_seeded(qew_ctx *ctx, int nx, int ny, double Lx, double Ly,
+                                  double amplitude, double xi_x, double xi_y, uint64_t seed,
+                                  int store_flags, qew_field **out) {
+    if (!ctx || !out || nx <= 0 || ny <= 0 || !(Lx > 0) || !(Ly > 0) ||
+        !std::isfinite(amplitude) || !std::isfinite(xi_x) || !std::isfinite(xi_y))
+        return qew_fail(ctx, QEW_ERR_INVALID, "field_create_seeded: bad arguments");
+    QEW_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t N = (size_t)nx * ny;
+    cufftDoubleComplex *spec = nullptr, *stage = nullptr;
+    double *w = nullptr;
+    cufftHandle plan = 0;
+    bool have_plan = false;
+    const int rows = std::max(1, std::min(nx, (1 << 20) / ny));  // host rows per upload
+    const size_t chunk = (size_t)rows * ny;
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    auto cleanup = [&](qew_status s) {
+        cudaStreamSynchronize(ctx->stream);
+        if (have_plan) cufftDestroy(plan);
+        for (cudaEvent_t &e : done)
+            if (e) cudaEventDestroy(e);
+        if (stage) cudaFreeHost(stage);
+        qew_free_async(spec, ctx->stream);
+        qew_free_async(w, ctx->stream);
+        return s;
+    };
+    if (qew_alloc_async(ctx, (void **)&spec, N * sizeof(cufftDoubleComplex)) != QEW_OK ||
+        qew_alloc_async(ctx, (void **)&w, N * sizeof(double) + 256) != QEW_OK ||
+        cudaMallocHost((void **)&stage, 2 * chunk * sizeof(cufftDoubleComplex)) != cudaSuccess)
+        return cleanup(qew_fail(ctx, QEW_ERR_NOMEM, "field_create_seeded: out of memory"));
+    for (cudaEvent_t &e : done)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+            return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "field_create_seeded: event"));
+    // Random unit phases masked to the correlation ellipse, drawn on the host in
+    // the reference's order (filtered_noise.cpp:37-53: i over nx outer, j inner,
+    // one draw per entry whether masked or not), uploaded in row chunks through
+    // two pinned buffers so drawing overlaps the copies.
+    const double two_pi = 2.0 * std::acos(-1.0);
+    const double dx = Lx / nx, dy = Ly / ny;
+    std::mt19937_64 rng(seed);
+    std::uniform_real_distribution<double> phase(0.0, two_pi);
+    for (int i0 = 0, b = 0; i0 < nx; i0 += rows, b ^= 1) {
+        const int i1 = std::min(nx, i0 + rows);
+        cufftDoubleComplex *hs = stage + (size_t)b * chunk;
+        if (cudaEventSynchronize(done[b]) != cudaSuccess)
+            return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "field_create_seeded: upload"));
+        for (int i = i0; i < i1; ++i) {
+            const double fx = fft_freq(i, nx) / dx;
+            for (int j = 0; j < ny; ++j) {
+                const double fy = fft_freq(j, ny) / dy;
+                const double ph = phase(rng);
+                cufftDoubleComplex a{0.0, 0.0};
+                if (!((fx * xi_x) * (fx * xi_x) + (fy * xi_y) * (fy * xi_y) > 1.0))
+                    a = cufftDoubleComplex{std::cos(ph), std::sin(ph)};
+                hs[(size_t)(i - i0) * ny + j] = a;
+            }
+        }
+        cudaError_t e = cudaMemcpyAsync(spec + (size_t)i0 * ny, hs,
+                                        (size_t)(i1 - i0) * ny * sizeof(cufftDoubleComplex),
+                                        cudaMemcpyHostToDevice, ctx->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(done[b], ctx->stream);
+        if (e != cudaSuccess) return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "%s", cudaGetErrorString(e)));
+    }
+    if (cufftPlan2d(&plan, nx, ny, CUFFT_Z2Z) != CUFFT_SUCCESS)
+        return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "cufftPlan2d Z2Z(%d, %d) failed", nx, ny));
+    have_plan = true;
+    if (cufftSetStream(plan, ctx->stream) != CUFFT_SUCCESS ||
+        cufftExecZ2Z(plan, spec, spec, CUFFT_INVERSE) != CUFFT_SUCCESS)
+        return cleanup(qew_fail(ctx, QEW_ERR_CUDA, "field_create_seeded: inverse FFT failed"));
+    double *scale = w + N;
+    k_real_part<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(spec, N, 1.0 / (double)N, w);
+    k_std_scale<<<1, 1024, 0, ctx->stream>>>(w, N, amplitude, scale);
+    k_scale_inplace<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(w, N, scale);
+    qew_status st = qew_launch_check(ctx, "field_seeded", 3);
+    if (st != QEW_OK) return cleanup(st);
+    return cleanup(field_build(ctx, w, true, nx, ny, Lx, Ly, store_flags, out));
 }
 
 qew_status qew_field_create_analytic(qew_ctx *ctx, int kind, double p0, double p1, double p2,
