@@ -57,7 +57,7 @@ def parse():
                     help="lines of the batched-statics section (0 skips it)")
     ap.add_argument("--ensemble-ref", type=int, default=16,
                     help="lines timed with the plain one-line-per-launch form")
-    ap.add_argument("--sections", default="ensemble,dynamics,depinning,serving",
+    ap.add_argument("--sections", default="static,ensemble,dynamics,depinning,serving",
                     help="extra configurations reported beside the headline")
     ap.add_argument("--dyn-steps", type=int, default=100000)
     ap.add_argument("--dyn-plain-steps", type=int, default=2000)
@@ -239,6 +239,77 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ------------------------------------------------------------- static (C0)
+def host_gaussian_field(nx, ny, xi, seed):
+    """Seeded N(0,1) white noise, Gaussian filter exp(-(2 pi xi f)^2 / 2) in
+    Fourier space (f in cycles per cell), unit population std; [nx][ny]."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((nx, ny))
+    fx = np.fft.fftfreq(nx)[:, None]
+    fy = np.fft.rfftfreq(ny)[None, :]
+    filt = np.exp(-0.5 * (2 * np.pi * xi) ** 2 * (fx ** 2 + fy ** 2))
+    f = np.fft.irfft2(np.fft.rfft2(w) * filt, s=(nx, ny))
+    return f / f.std()
+
+
+def run_static(args, Q, torch):
+    """C0: L = 1024, linear elasticity of stiffness 1, 1024 x 1024 field
+    (seed 0, xi in {2, 4, 8} cells, unit variance), h0 = 0, L-BFGS m = 10
+    with the preconditioner (shift 0.5 dx A / xi^2), to max|g| < 1e-8 — on
+    the GPU (resident form) and with the CPU oracle (serial), the same field
+    coefficients on both sides. With the reference's Armijo search alone the
+    solve can stall just above 1e-8 (energy differences below the energy's
+    rounding); the approximate-Wolfe fallback is on for both sides, and the
+    Armijo-only GPU run is reported beside it."""
+    from oracle import oracle as O
+    n = 1024
+    out = {"metric": "static solves/s at max|g| < 1e-8", "unit": "solves/s",
+           "workload": "L=1024, 1024x1024 field seed 0, xi in {2,4,8}, linear, h0=0, m=10, "
+                       "preconditioned", "xi": {}}
+    gpu_total = cpu_total = 0.0
+    for xi in (2.0, 4.0, 8.0):
+        field = host_gaussian_field(n, n, xi, 0)
+        f = Q.FilteredNoise(field, float(n), float(n))
+        p = Q.Params(float(n), 1.0, 0.0, Q.Model.Linear)
+        shift = 0.5 * 1.0 * 1.0 / xi ** 2
+        lp = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=20000, precondition=True,
+                           precond_shift=shift, ls_fallback=True)
+        h = torch.zeros(n, dtype=torch.float64, device="cuda")
+        Q.lbfgs_minimize(h.clone(), p, f, lp)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = Q.lbfgs_minimize(h, p, f, lp)
+        torch.cuda.synchronize()
+        tg = time.perf_counter() - t0
+        e_gpu = Q.objective(h, p, f)
+        h_ref = torch.zeros(n, dtype=torch.float64, device="cuda")
+        lp_ref = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=20000, precondition=True,
+                               precond_shift=shift)
+        rr = Q.lbfgs_minimize(h_ref, p, f, lp_ref)
+        of = O.BSplineField(field, float(n), float(n), coef=f.coefficients())
+        hc = np.zeros(n)
+        op = O.params(float(n), 1.0, 0.0, 0)
+        olp = O.lbfgs_default_params(m=10, ftol=1e-8, max_iter=20000, precondition=1,
+                                     precond_shift=shift, ls_fallback=1)
+        t0 = time.perf_counter()
+        rc = O.lbfgs_minimize(hc, op, of, olp)
+        tc = time.perf_counter() - t0
+        e_cpu = O.objective(hc, op, of)
+        gpu_total += tg
+        cpu_total += tc
+        out["xi"][str(int(xi))] = {
+            "gpu_s": tg, "gpu_iterations": r.iterations, "gpu_max_grad": r.max_force,
+            "gpu_converged": bool(r.converged), "cpu_s": tc, "cpu_iterations": rc.iterations,
+            "cpu_max_grad": rc.max_force, "cpu_converged": bool(rc.converged),
+            "energy_rel_diff": abs(e_gpu - e_cpu) / abs(e_cpu),
+            "armijo_only_gpu": {"iterations": rr.iterations, "max_grad": rr.max_force,
+                                "converged": bool(rr.converged)}}
+    out["value"] = 3.0 / gpu_total
+    out["cpu_solves_per_s"] = 3.0 / cpu_total
+    out["cpu"] = {"cores": 1, "kind": "port", "sample": "the three solves, serial oracle"}
+    return out
 
 
 # ----------------------------------------------------------- ensemble (C3)
@@ -576,36 +647,43 @@ def run_ours(args):
     roof_fp64 = roofline(t2_ms if headline_split else t_ms,
                          launches2 if headline_split else launches, 48.0, "k_gradient")
     # DRAM bytes (read + write) per line point from one ncu capture of each
-    # kernel on a single 2^20-point line of this workload's kind, scaled to
-    # the points of one launch (traffic grows in proportion to the points).
+    # kernel: the split gather's batched launch (8 lines of 2^20 points, 256-row
+    # field: 241.549056 MB read + 20.686080 MB written) and the FP64 gather on
+    # one 2^20-point line (53.188352 MB), scaled to the points of one launch
+    # (traffic grows in proportion to the points).
     pts_split = args.steps * n_inst * L / max(launches if headline_split else launches2, 1)
     pts_fp64 = args.steps * n_inst * L / max(launches2 if headline_split else launches, 1)
-    roof_split["traffic"] = 35.224832e6 / L_FULL * pts_split
+    roof_split["traffic"] = (241.549056e6 + 20.686080e6) / (8 * L_FULL) * pts_split
     roof_fp64["traffic"] = 53.188352e6 / L_FULL * pts_fp64
 
     e2e = None
     cpu = None
     if not args.profile_run:
         prec = Q.QEW_PREC_FP32_SPLIT if headline_split else Q.QEW_PREC_FP64
-        hh = [torch.as_tensor(h).pin_memory().numpy() for h in hs_host]
-        gh = [torch.empty(L, dtype=torch.float64).pin_memory().numpy() for _ in range(n_inst)]
-        for k in range(n_inst):
-            Q.gradient_host(hh[k], p, noise, gh[k], precision=prec)
+        hh = torch.as_tensor(np.stack(hs_host)).pin_memory().numpy()
+        gh = torch.empty((n_inst, L), dtype=torch.float64).pin_memory().numpy()
+        for _ in range(2):
+            Q.gradient_host_batch(hh, p, noise, gh, precision=prec)
         torch.cuda.synchronize()
-        e2e_steps = max(2, args.steps // 2)
+        e2e_steps = max(3, args.steps // 2)
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            for k in range(n_inst):
-                Q.gradient_host(hh[k], p, noise, gh[k], precision=prec)
+            Q.gradient_host_batch(hh, p, noise, gh, precision=prec)
         dt = time.perf_counter() - t0
         e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
                "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
-               "call": "qew_gradient_host (FP64 host heights in, FP64 host gradient out)"}
-    ensemble = dynamics = depinning = serving = None
+               "call": "qew_gradient_host_batch: the step's 8 lines as FP64 pinned host heights "
+                       "in, FP64 host gradients out (uploads, gradients and downloads of "
+                       "consecutive lines overlapped)"}
+    static = ensemble = dynamics = depinning = serving = None
     sections = set(s.strip() for s in args.sections.split(",") if s.strip())
     if not args.profile_run and sections:
         del noise, cells, fracs, g32, g64, hs
         torch.cuda.empty_cache()
+        if "static" in sections:
+            log("static section")
+            static = run_static(args, Q, torch)
+            torch.cuda.empty_cache()
         if "ensemble" in sections and args.ensemble_lines > 0:
             log("ensemble section")
             ensemble = run_ensemble(args, Q, torch)
@@ -643,7 +721,7 @@ def run_ours(args):
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "roofline": roof_split if headline_split else roof_fp64,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-                "other_precision": other, "ensemble": ensemble, "dynamics": dynamics,
+                "other_precision": other, "static": static, "ensemble": ensemble, "dynamics": dynamics,
                 "depinning": depinning, "serving": serving}
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -225,6 +225,15 @@ qew_status qew_gradient_prec(qew_ctx *ctx, const qew_field *field,
 qew_status qew_gradient_host(qew_ctx *ctx, const qew_field *field,
                              const double *h_h, int n, const qew_params *p,
                              int precision, double *h_grad);
+/* Gradients of `count` host lines (h_h and h_grad hold count * n doubles,
+ * line k at k * n; pinned memory lets the copies run asynchronously) in one
+ * call: uploads, gradients and downloads of consecutive lines overlap on
+ * three streams. No reference counterpart (the reference computes one
+ * device-resident line per gradient() call, qew_model.h:149-201). */
+qew_status qew_gradient_host_batch(qew_ctx *ctx, const qew_field *field,
+                                   int count, const double *h_h, int n,
+                                   const qew_params *p, int precision,
+                                   double *h_grad);
 
 /* FP32 split-index form of the gather (the bandwidth form; no reference
  * counterpart). Heights are carried in field y-cells as an integer cell plus

@@ -44,7 +44,7 @@ from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # n
 __all__ = [
     "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
     "SinusoidNoise", "AnalyticNoise", "objective", "objective_trial", "gradient",
-    "gradient_host", "split_heights", "join_heights", "gradient_split", "gradient_split_batch",
+    "gradient_host", "gradient_host_batch", "split_heights", "join_heights", "gradient_split", "gradient_split_batch",
     "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "ensemble_minimize",
     "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
@@ -382,6 +382,26 @@ def gradient_host(h: np.ndarray, p: Params, noise: _Noise, out: np.ndarray | Non
     _capi.check(ctx.lib.qew_gradient_host(ctx.h, noise.h, C.c_void_p(h.ctypes.data), h.size,
                                           C.byref(pc), precision, C.c_void_p(out.ctypes.data)),
                 ctx.h, "gradient_host")
+    return out
+
+
+def gradient_host_batch(h: np.ndarray, p: Params, noise: _Noise, out: np.ndarray | None = None,
+                        precision: int = QEW_PREC_FP64) -> np.ndarray:
+    """Gradients of the rows of a host array h[count, n] (ideally pinned), the
+    copies of consecutive rows overlapped with the gradients on the device."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    h = np.ascontiguousarray(h, dtype=np.float64)
+    if h.ndim != 2:
+        raise ValueError("h must be [count, n]")
+    if out is None:
+        out = np.empty_like(h)
+    pc = p.c()
+    _capi.check(ctx.lib.qew_gradient_host_batch(ctx.h, noise.h, h.shape[0],
+                                                C.c_void_p(h.ctypes.data), h.shape[1],
+                                                C.byref(pc), precision,
+                                                C.c_void_p(out.ctypes.data)),
+                ctx.h, "gradient_host_batch")
     return out
 
 

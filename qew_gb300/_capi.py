@@ -154,6 +154,7 @@ _SIGS = {
     "qew_gradient": (I, [VP, VP, VP, I, C.POINTER(qew_params), VP]),
     "qew_gradient_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_gradient_host": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
+    "qew_gradient_host_batch": (I, [VP, VP, I, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_split_heights": (I, [VP, VP, VP, I, VP, VP]),
     "qew_join_heights": (I, [VP, VP, VP, VP, I, VP]),
     "qew_gradient_split": (I, [VP, VP, VP, VP, I, C.POINTER(qew_params), VP]),

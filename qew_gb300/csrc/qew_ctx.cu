@@ -116,6 +116,15 @@ qew_status qew_ctx_destroy(qew_ctx *ctx) {
     if (ctx->host_out) cudaFreeHost(ctx->host_out);
     if (ctx->scratch) cudaFreeAsync(ctx->scratch, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
+    for (cudaStream_t s : {ctx->copy_in, ctx->copy_out})
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    for (int k = 0; k < 3; ++k)
+        for (cudaEvent_t e : {ctx->ev_in[k], ctx->ev_comp[k], ctx->ev_out[k]})
+            if (e) cudaEventDestroy(e);
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     delete ctx;
     return QEW_OK;
 }

@@ -35,6 +35,10 @@ struct qew_ctx {
     size_t scratch_bytes = 0;
     uint64_t launches = 0;
     std::string last_error;
+    // copy streams and slot events of the host-buffer batch pipeline
+    // (created on first use)
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t ev_in[3] = {}, ev_comp[3] = {}, ev_out[3] = {}, ev_start = nullptr;
 };
 
 struct qew_field {

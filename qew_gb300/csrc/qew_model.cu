@@ -105,4 +105,60 @@ qew_status qew_gradient_host(qew_ctx *ctx, const qew_field *field, const double 
     return QEW_OK;
 }
 
+// Lines k = 0..count-1 of h_h (n apart) through three device slots: the
+// upload of line k, the gradient of line k-1 and the download of line k-2 run
+// at the same time on three streams (copy_in, ctx->stream, copy_out), ordered
+// by per-slot events, so the host link carries both directions at once.
+qew_status qew_gradient_host_batch(qew_ctx *ctx, const qew_field *field, int count,
+                                   const double *h_h, int n, const qew_params *p, int precision,
+                                   double *h_grad) {
+    if (!ctx || !h_h || !h_grad || n < 1 || count < 0)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient_host_batch: bad arguments");
+    if (count == 0) return QEW_OK;
+    QEW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!ctx->copy_in) {
+        QEW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
+        QEW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));
+        QEW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_start, cudaEventDisableTiming));
+        for (int s = 0; s < 3; ++s) {
+            QEW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_in[s], cudaEventDisableTiming));
+            QEW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_comp[s], cudaEventDisableTiming));
+            QEW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_out[s], cudaEventDisableTiming));
+        }
+    }
+    constexpr int S = 3;
+    const size_t bytes = sizeof(double) * (size_t)n;
+    const size_t npad = ((size_t)n + 31) & ~size_t(31);
+    QEW_TRY(qew_scratch_reserve(ctx, 2 * S * npad * sizeof(double) + 256));
+    double *dh[S], *dg[S];
+    for (int s = 0; s < S; ++s) {
+        dh[s] = (double *)ctx->scratch + (size_t)(2 * s) * npad;
+        dg[s] = (double *)ctx->scratch + (size_t)(2 * s + 1) * npad;
+    }
+    // the copy streams start after everything already queued on ctx->stream
+    QEW_CUDA(ctx, cudaEventRecord(ctx->ev_start, ctx->stream));
+    QEW_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->ev_start, 0));
+    QEW_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ctx->ev_start, 0));
+    for (int k = 0; k < count; ++k) {
+        const int s = k % S;
+        if (k >= S) QEW_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_in, ctx->ev_comp[s], 0));
+        QEW_CUDA(ctx, cudaMemcpyAsync(dh[s], h_h + (size_t)k * n, bytes, cudaMemcpyHostToDevice,
+                                      ctx->copy_in));
+        QEW_CUDA(ctx, cudaEventRecord(ctx->ev_in[s], ctx->copy_in));
+        QEW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_in[s], 0));
+        if (k >= S) QEW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_out[s], 0));
+        QEW_TRY(qew_gradient_enqueue(ctx, field, dh[s], n, p, precision, dg[s]));
+        QEW_CUDA(ctx, cudaEventRecord(ctx->ev_comp[s], ctx->stream));
+        QEW_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_out, ctx->ev_comp[s], 0));
+        QEW_CUDA(ctx, cudaMemcpyAsync(h_grad + (size_t)k * n, dg[s], bytes, cudaMemcpyDeviceToHost,
+                                      ctx->copy_out));
+        QEW_CUDA(ctx, cudaEventRecord(ctx->ev_out[s], ctx->copy_out));
+    }
+    // later work on ctx->stream (scratch reuse) follows the last download
+    QEW_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_out[(count - 1) % S], 0));
+    QEW_CUDA(ctx, cudaStreamSynchronize(ctx->copy_out));
+    QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return QEW_OK;
+}
+
 }  // extern "C"

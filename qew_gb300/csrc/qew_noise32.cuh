@@ -42,9 +42,6 @@ struct NoiseSplit32 {
         fy = (float)f;
     }
     __device__ __forceinline__ float taps(int ix, float fx, int iy, float fy, bool deriv) const {
-        int xs[4], ys[4];
-        wrap4(ix, nx, xs);
-        wrap4(iy, ny, ys);
         float wx[4], wy[4];
         bsw_value32(fx, wx);
         if (deriv)
@@ -52,6 +49,22 @@ struct NoiseSplit32 {
         else
             bsw_value32(fy, wy);
         float acc = 0.0f;
+        if (ix >= 1 && ix <= nx - 3 && iy >= 1 && iy <= ny - 3) {
+            // no wrap on either axis: one base pointer, taps at fixed offsets
+            // (the same sum in the same order as below)
+            const float *p = coef + ((size_t)(iy - 1) * (size_t)nx + (size_t)(ix - 1));
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const float *row = p + (size_t)b * (size_t)nx;
+                const float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) +
+                                wx[2] * __ldg(row + 2) + wx[3] * __ldg(row + 3);
+                acc += wy[b] * r;
+            }
+            return acc;
+        }
+        int xs[4], ys[4];
+        wrap4(ix, nx, xs);
+        wrap4(iy, ny, ys);
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
             const float *row = coef + (size_t)ys[b] * (size_t)nx;

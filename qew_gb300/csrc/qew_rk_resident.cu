@@ -2,9 +2,10 @@
 // cooperative kernel: all sweeps, both colours and the per-sweep verdict run
 // on the device, with a grid barrier between colours instead of a kernel
 // launch, and the sweep's total advance reduced deterministically (per-CTA
-// partials summed in CTA order by every CTA). The per-site arithmetic is
-// exactly the host-driven form's (qew_rk_device.cuh), so both forms produce
-// bit-identical lines.
+// partials summed in CTA order by every CTA). Each site's forward zero is
+// evaluated by a group of lanes (rk_forward_zero_group: several march points
+// or bisection levels per round) that replays the serial search exactly, so
+// both forms produce bit-identical lines.
 //
 // The grid barrier spins on a generation word with a bounded number of polls;
 // if it gives up it raises an error flag, every CTA leaves the sweep loop, and
@@ -23,6 +24,7 @@
 namespace {
 
 constexpr int kRkBS = 32;  // one warp per CTA: a 16384-site line still spreads over every SM
+constexpr int kRkGroup = 8;  // lanes per site: 7 march points or 3 bisection levels per round
 template <class Noise>
 __global__ void __launch_bounds__(kRkBS)
 k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n, double dx,
@@ -32,6 +34,9 @@ k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n,
     const int gtid = blockIdx.x * kRkBS + threadIdx.x;
     const int gstride = nb * kRkBS;
     const int half = n / 2;
+    const int glane = threadIdx.x & (kRkGroup - 1);
+    const unsigned gmask = ((kRkGroup == 32) ? 0xffffffffu : ((1u << kRkGroup) - 1u))
+                           << ((threadIdx.x & 31) & ~(kRkGroup - 1));
     __shared__ double s_w[kRkBS / 32];
     // mean(h) at entry (rosso_krauth.h:144-148)
     double acc = 0.0;
@@ -48,18 +53,23 @@ k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n,
     for (int sweep = 0; sweep < rp.max_sweeps; ++sweep) {
         double local = 0.0;
         for (int color = 0; color < 2; ++color) {
-            for (int k = gtid; k < half; k += gstride) {
+            // one group of kRkGroup lanes per site of this colour
+            for (int k = gtid / kRkGroup; k < half; k += gstride / kRkGroup) {
                 const int i = 2 * k + color;
                 const int im = (i == 0) ? n - 1 : i - 1;
                 const int ip = (i + 1 == n) ? 0 : i + 1;
                 bool found = false;
                 const double hi = __ldcg(h + i);
-                const double hnew = rk_forward_zero(nz, i, n, dx, lt, f, model, hi, __ldcg(h + im),
-                                                    __ldcg(h + ip), rp, found);
-                const double a = hnew - hi;
-                adv[i] = a;
-                h[i] = hnew;
-                local += a;
+                const double hnew = rk_forward_zero_group<kRkGroup>(
+                    nz, i, n, dx, lt, f, model, hi, __ldcg(h + im), __ldcg(h + ip), rp, found,
+                    glane, gmask);
+                __syncwarp(gmask);  // every lane has read h[i]
+                if (glane == 0) {
+                    const double a = hnew - hi;
+                    adv[i] = a;
+                    h[i] = hnew;
+                    local += a;
+                }
             }
             if (color == 0 && !grid_sync_bounded(sync, nb)) return;
         }
@@ -100,7 +110,7 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
     auto launch = [&](auto nz) -> qew_status {
         auto kern = k_rk_resident<decltype(nz)>;
         QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, kern, kRkBS, 0));
-        const int want = (n / 2 + kRkBS - 1) / kRkBS;
+        const int want = (int)(((long long)(n / 2) * kRkGroup + kRkBS - 1) / kRkBS);
         const int grid = std::max(1, std::min(want, ctx->num_sms * std::max(max_per_sm, 1)));
         // scratch: adv[n], partials[3*grid], sync word, result
         const size_t off_part = ((size_t)n * sizeof(double) + 255) & ~size_t(255);

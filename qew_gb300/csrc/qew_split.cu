@@ -91,6 +91,27 @@ __device__ __forceinline__ float split_dvdy(const float *__restrict__ coef, int 
     return dg * inv_dy;
 }
 
+// The same sum for a stencil that wraps neither axis (1 <= ix <= nx - 3,
+// 1 <= cy <= ny - 3, true for all but the edge cells): one base pointer, the
+// 16 taps at fixed offsets from it, no wrap arithmetic. Same operations in the
+// same order as split_dvdy, so the result is identical.
+__device__ __forceinline__ float split_dvdy_interior(const float *__restrict__ coef, int nx,
+                                                     int ix, const float wx[4], int cy, float fy,
+                                                     float inv_dy) {
+    float dwy[4];
+    bsw_deriv_f(fy, dwy);
+    const float *p = coef + ((size_t)(cy - 1) * (size_t)nx + (size_t)(ix - 1));
+    float dg = 0.0f;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+        const float *row = p + (size_t)b * (size_t)nx;
+        const float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) + wx[2] * __ldg(row + 2) +
+                        wx[3] * __ldg(row + 3);
+        dg += dwy[b] * r;
+    }
+    return dg * inv_dy;
+}
+
 // Midpoint of two split heights: (c0 + f0 + c1 + f1) / 2 as (cell, frac).
 __device__ __forceinline__ void split_mid(int c0, float f0, int c1, float f1, int &cm, float &fm) {
     const int C = c0 + c1;
@@ -107,12 +128,20 @@ __device__ __forceinline__ void split_mid(int c0, float f0, int c1, float f1, in
 // One CTA covers a tile of kTile = kBS * kItems consecutive sites of one line
 // (blockIdx.y selects the line of a batch stored contiguously, n apart).
 // Thread t owns sites t, t + kBS, ... of the tile, so every load phase is
-// coalesced, and each thread keeps 4 x 16 independent gathers in flight.
-constexpr int kItems = 4;
+// coalesced, and each thread keeps kItems x 16 independent gathers in flight.
+// Sites per thread and the resident-CTA hint are build-time tuning knobs
+// (chosen by measurement on GB300; see the build's flags).
+#ifndef QEW_SPLIT_ITEMS
+#define QEW_SPLIT_ITEMS 2
+#endif
+#ifndef QEW_SPLIT_MIN_CTAS
+#define QEW_SPLIT_MIN_CTAS 8
+#endif
+constexpr int kItems = QEW_SPLIT_ITEMS;
 constexpr int kTile = kBS * kItems;
 
 template <bool IN64, bool OUT64>
-__global__ void __launch_bounds__(kBS)
+__global__ void __launch_bounds__(kBS, QEW_SPLIT_MIN_CTAS)
 k_gradient_split(const double *__restrict__ h64, const int *__restrict__ hc,
                  const float *__restrict__ hf, SplitGeom g, double *__restrict__ grad64,
                  float *__restrict__ grad32) {
@@ -148,12 +177,25 @@ k_gradient_split(const double *__restrict__ h64, const int *__restrict__ hc,
     if (t == kBS - 1) load((base + cnt == n) ? 0 : base + cnt, cnt + 1);
     __syncthreads();
     const bool arc = g.arc;
+    float wx_half[4];  // x weights at fx = 1/2, every edge but the wrap edge on a shared grid
+    bsw_value_f(0.5f, wx_half);
     auto edge = [&](int e, int sl, int sr, int out) {
         int ix, cm;
         float fx, fm;
         edge_x(g, e, ix, fx);
         split_mid(s_c[sl], s_f[sl], s_c[sr], s_f[sr], cm, fm);
-        s_dv[out] = split_dvdy(g.coef, g.nx, g.ny, ix, fx, cm, fm, g.inv_dy_f);
+        if (ix >= 1 && ix <= g.nx - 3 && cm >= 1 && cm <= g.ny - 3) {
+            float wx[4];
+            if (g.same_grid && e + 1 < n) {
+#pragma unroll
+                for (int a = 0; a < 4; ++a) wx[a] = wx_half[a];
+            } else {
+                bsw_value_f(fx, wx);
+            }
+            s_dv[out] = split_dvdy_interior(g.coef, g.nx, ix, wx, cm, fm, g.inv_dy_f);
+        } else {
+            s_dv[out] = split_dvdy(g.coef, g.nx, g.ny, ix, fx, cm, fm, g.inv_dy_f);
+        }
         if (arc) {
             const float dh = ((float)(s_c[sr] - s_c[sl]) + (s_f[sr] - s_f[sl])) * g.dy_over_dx;
             s_sl[out] = dh * rsqrtf(1.0f + dh * dh);
@@ -226,6 +268,16 @@ SplitGeom qew_split_geom(const qew_field *f, int n, const qew_params *p) {
     return g;
 }
 
+// Split heights in, FP32 gradient out, `count` lines n apart.
+static qew_status split_launch(qew_ctx *ctx, const qew_field *f, const SplitGeom &g, int count,
+                               const int32_t *d_cell, const float *d_frac, float *d_grad,
+                               const char *what) {
+    (void)f;
+    k_gradient_split<false, false><<<dim3((g.n + kTile - 1) / kTile, count), kBS, 0, ctx->stream>>>(
+        nullptr, d_cell, d_frac, g, nullptr, d_grad);
+    return qew_launch_check(ctx, what);
+}
+
 static qew_status split_check(qew_ctx *ctx, const qew_field *f, int n, const qew_params *p) {
     if (!ctx || !f || !p || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "split gradient: bad arguments");
@@ -268,10 +320,8 @@ qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *f, const int32_t *d
     QEW_TRY(split_check(ctx, f, n, p));
     if (!d_cell || !d_frac || !d_grad)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split: null buffer");
-    const SplitGeom g = qew_split_geom(f, n, p);
-    k_gradient_split<false, false><<<dim3((n + kTile - 1) / kTile, 1), kBS, 0, ctx->stream>>>(
-        nullptr, d_cell, d_frac, g, nullptr, d_grad);
-    return qew_launch_check(ctx, "gradient_split");
+    return split_launch(ctx, f, qew_split_geom(f, n, p), 1, d_cell, d_frac, d_grad,
+                        "gradient_split");
 }
 
 qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *f, int count,
@@ -280,10 +330,8 @@ qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *f, int count,
     QEW_TRY(split_check(ctx, f, n, p));
     if (!d_cell || !d_frac || !d_grad || count < 1 || count > 65535)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split_batch: bad arguments");
-    const SplitGeom g = qew_split_geom(f, n, p);
-    k_gradient_split<false, false><<<dim3((n + kTile - 1) / kTile, count), kBS, 0, ctx->stream>>>(
-        nullptr, d_cell, d_frac, g, nullptr, d_grad);
-    return qew_launch_check(ctx, "gradient_split_batch");
+    return split_launch(ctx, f, qew_split_geom(f, n, p), count, d_cell, d_frac, d_grad,
+                        "gradient_split_batch");
 }
 
 }  // extern "C"

@@ -162,3 +162,20 @@ def test_gradient_host_roundtrip(Q, O):
     g_host = Q.gradient_host(h, p, f)
     g_dev = npy(Q.gradient(t64(h), p, f))
     assert np.array_equal(g_host, g_dev)
+
+
+@pytest.mark.parametrize("count", [1, 2, 3, 7])
+def test_gradient_host_batch_equals_single_calls(Q, count):
+    """The pipelined batch gives every line exactly what one call per line gives,
+    for batches shorter and longer than its three device slots."""
+    import torch
+    n = 3001
+    f = Q.FilteredNoise(band_limited_field(500, 32, 50.0, 1.0, 1.0, 0.5, 4), 50.0, 1.0,
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    rng = np.random.default_rng(count)
+    h = torch.as_tensor(rng.uniform(0, 1, (count, n))).pin_memory().numpy()
+    p = Q.Params(50.0, 1.0, 0.1, Q.Model.Arclength)
+    for prec in (Q.QEW_PREC_FP64, Q.QEW_PREC_FP32_SPLIT):
+        out = Q.gradient_host_batch(h, p, f, precision=prec)
+        for k in range(count):
+            assert np.array_equal(out[k], Q.gradient_host(h[k].copy(), p, f, precision=prec))

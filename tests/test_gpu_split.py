@@ -110,3 +110,28 @@ def test_split_batch_equals_single_lines(Q):
         for k in range(count):
             gk = npy(Q.gradient_split(sp[k][0], sp[k][1], p, f))
             assert np.array_equal(gb[k], gk)
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("n, nx, ny, rough", [
+    (4096, 4096, 64, 0.2),     # shared grid, smooth line
+    (4096, 4096, 64, 30.0),    # rough line wrapping around the field many times
+    (3000, 2048, 48, 0.5),     # line and field grids differ
+    (2048, 2046, 40, 0.3),     # odd row pitch
+])
+def test_split_heights_form_equals_fp64_input_form(Q, model, n, nx, ny, rough):
+    """Split heights -> FP32 gradient equals the same gather fed FP64 heights
+    (split inside the kernel), bitwise after rounding its FP64 output to FP32,
+    including the interior fast path, the wrap-around stencils and both
+    x-geometries."""
+    Lx = float(nx)
+    f = Q.FilteredNoise(gaussian_field(nx, ny, 3.0, 21), Lx, float(ny),
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    rng = np.random.default_rng(n + nx)
+    h = t64(ny / 2 + np.cumsum(rng.standard_normal(n)) * rough * 0.1 + 0.3 * ny * np.sin(
+        np.linspace(0, 2 * np.pi, n, endpoint=False)))
+    p = Q.Params(Lx, 0.9, 0.02, Q.Model(model))
+    cell, frac = Q.split_heights(h, f)
+    g_split = npy(Q.gradient_split(cell, frac, p, f))
+    g_in64 = npy(Q.gradient(h, p, f, precision=Q.QEW_PREC_FP32_SPLIT)).astype(np.float32)
+    assert np.array_equal(g_split, g_in64)
