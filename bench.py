@@ -206,6 +206,15 @@ def cpu_gradient_rate(seconds: float, L: int = L_FULL, ny: int = 64):
                       "(OpenMP, %.1f s)" % (reps, ny, dt)}
 
 
+def headline_config(L, ny, n_inst, precision, ws):
+    """The headline workload's description (both arms print the same)."""
+    return {"workload": "gradient of %d line instances of L=2^20 points on a 2^20x%d field "
+                        "(xi=4 cells), %s gather" % (n_inst, ny, precision),
+            "L": L, "rows": ny, "instances_per_step": n_inst, "model": "linear",
+            "l2": "inputs larger than L2 (8 disjoint row bands per step)",
+            "parallelism": "replicas" if ws > 1 else "single GPU"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -229,12 +238,13 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "gradient of a 2^20-point line, FP64, CPU oracle (reference "
-                                   "algorithm restated), 2^20x64-row sample field",
-                       "L": L, "rows": ny},
+            "config": headline_config(L, NY_FULL, N_INST, args.precision, 1),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": O.omp_max_threads(),
                              "kind": "port",
-                             "sample": "one 2^20-point gradient per step, OpenMP"},
+                             "sample": "per step one of the workload's 2^20-point lines (FP64, the "
+                                       "reference algorithm restated in the CPU oracle, OpenMP) "
+                                       "on a 2^20x64 field: the gather's cost does not depend "
+                                       "on the field height"},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -648,12 +658,12 @@ def run_ours(args):
                          launches2 if headline_split else launches, 48.0, "k_gradient")
     # DRAM bytes (read + write) per line point from one ncu capture of each
     # kernel: the split gather's batched launch (8 lines of 2^20 points, 256-row
-    # field: 241.549056 MB read + 20.686080 MB written) and the FP64 gather on
+    # field: 241.858816 MB read + 20.879104 MB written) and the FP64 gather on
     # one 2^20-point line (53.188352 MB), scaled to the points of one launch
     # (traffic grows in proportion to the points).
     pts_split = args.steps * n_inst * L / max(launches if headline_split else launches2, 1)
     pts_fp64 = args.steps * n_inst * L / max(launches2 if headline_split else launches, 1)
-    roof_split["traffic"] = (241.549056e6 + 20.686080e6) / (8 * L_FULL) * pts_split
+    roof_split["traffic"] = (241.858816e6 + 20.879104e6) / (8 * L_FULL) * pts_split
     roof_fp64["traffic"] = 53.188352e6 / L_FULL * pts_fp64
 
     e2e = None
@@ -712,13 +722,7 @@ def run_ours(args):
                 "steps": args.steps, "warmup": warm, "ms_per_step": t_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32" if headline_split else "f64", "data": "synthetic",
-                "config": {"workload": "gradient of %d line instances of L=2^20 points on a "
-                                       "2^20x%d field (xi=4 cells), %s gather"
-                                       % (n_inst, ny, args.precision),
-                           "L": L, "rows": ny, "instances_per_step": n_inst,
-                           "model": "linear",
-                           "l2": "inputs larger than L2 (8 disjoint row bands per step)",
-                           "parallelism": "replicas" if ws > 1 else "single GPU"},
+                "config": headline_config(L, ny, n_inst, args.precision, ws),
                 "roofline": roof_split if headline_split else roof_fp64,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "other_precision": other, "static": static, "ensemble": ensemble, "dynamics": dynamics,

@@ -294,6 +294,54 @@ qew_status qew_precond_apply(qew_ctx *ctx, const double *d_q, int n,
                              double line_tension, double physical_size,
                              double shift, int form, double *d_out);
 
+/* ------------------------------------------------------------------- FIRE */
+/* FireParams, fire.h:21-31 (same fields, same defaults; dt_max is required). */
+typedef struct {
+    double dt_max;
+    double dt_init;     /* <= 0: 0.1 * dt_max */
+    double ftol;
+    int max_iter;
+    int n_min;
+    double f_inc;
+    double f_dec;
+    double alpha_start;
+    double f_alpha;
+} qew_fire_params;
+
+/* FireResult, fire.h:33-37 */
+typedef struct {
+    int iterations;
+    double max_force;
+    int converged;
+} qew_fire_result;
+
+qew_status qew_fire_default_params(qew_fire_params *fp);
+/* fire_minimize(h, p, noise, fp), fire.h:41-131; relaxes d_h in place (one
+ * kernel, one CTA). */
+qew_status qew_fire_minimize(qew_ctx *ctx, const qew_field *field, double *d_h,
+                             int n, const qew_params *p,
+                             const qew_fire_params *fp, qew_fire_result *res);
+
+/* ------------------------------------------------------------- statistics */
+/* Roughness statistics of `count` periodic lines of n points (line k at
+ * d_h + k * n, physical length L), the datasets the reference's
+ * post-processing adds beside each profile (tools/postprocess_static.py:38-46:
+ * ell, acf, q, psd). Its routines live in an external package that is not in
+ * the reference tree, so the definitions are this project's, stated here:
+ *   dx = L / n,  H_k = sum_i h_i exp(-2 pi i i k / n),  k = 0 .. n/2
+ *   ell_k = k dx,  acf_k = (1/n) sum_i (h_{(i+k) mod n} - h_i)^2
+ *   q_k = 2 pi k / L,  psd_k = (dx / n) |H_k|^2
+ * Outputs (device): d_ell[n/2+1], d_acf[count][n/2+1], d_q[n/2+1],
+ * d_psd[count][n/2+1]; any of d_ell, d_q and one of d_acf / d_psd may be
+ * NULL. Transforms by cuFFT, batched over the lines. */
+qew_status qew_line_statistics(qew_ctx *ctx, int count, const double *d_h, int n,
+                               double physical_size, double *d_ell,
+                               double *d_acf, double *d_q, double *d_psd);
+/* The same from and to host arrays (h_h: count * n doubles). */
+qew_status qew_line_statistics_host(qew_ctx *ctx, int count, const double *h_h,
+                                    int n, double physical_size, double *h_ell,
+                                    double *h_acf, double *h_q, double *h_psd);
+
 /* --------------------------------------------------------------- ensemble */
 /* Batched statics (no reference counterpart: the reference relaxes one line
  * per lbfgs_minimize call, lbfgs.h:94-96). One entry per independent line. */

@@ -46,6 +46,15 @@ class QoLbfgsResult(C.Structure):
                 ("n_ls_restarts", C.c_long)]
 
 
+class QoFireParams(C.Structure):
+    _fields_ = [("dt_max", D), ("dt_init", D), ("ftol", D), ("max_iter", I), ("n_min", I),
+                ("f_inc", D), ("f_dec", D), ("alpha_start", D), ("f_alpha", D)]
+
+
+class QoFireResult(C.Structure):
+    _fields_ = [("iterations", I), ("max_force", D), ("converged", I)]
+
+
 class QoRkParams(C.Structure):
     _fields_ = [("dstep", D), ("max_advance", D), ("root_tol", D),
                 ("sweep_tol", D), ("runaway", D), ("max_sweeps", I)]
@@ -92,6 +101,8 @@ def lib():
                                           PD, PD, PD, C.POINTER(I)]
         L.qo_depinning_bisect.restype = I
         L.qo_philox_normals.argtypes = [C.c_uint64, C.c_uint64, I, PD]
+        L.qo_fire_minimize.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
+                                       C.POINTER(QoFireParams), C.POINTER(QoFireResult)]
         L.qo_mt64_seed.argtypes = [C.c_void_p, C.c_uint64]
         L.qo_mt64_next.argtypes = [C.c_void_p]
         L.qo_mt64_next.restype = C.c_uint64
@@ -289,3 +300,19 @@ def seeded_field(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed) -> np.ndarray:
     if lib().qo_seeded_field(nx, ny, Lx, Ly, amplitude, xi_x, xi_y, seed, _p(out)) != 0:
         raise MemoryError("qo_seeded_field")
     return out
+
+
+def fire_params(dt_max, **kw) -> QoFireParams:
+    """FireParams with the defaults of fire.h:21-31."""
+    fp = QoFireParams(float(dt_max), 0.0, 1e-6, 100000, 5, 1.1, 0.5, 0.1, 0.99)
+    for k, v in kw.items():
+        setattr(fp, k, v)
+    return fp
+
+
+def fire_minimize(h: np.ndarray, p: QoParams, noise: Noise, fp: QoFireParams) -> QoFireResult:
+    """Relaxes h in place (numpy float64)."""
+    assert h.dtype == np.float64 and h.flags["C_CONTIGUOUS"]
+    res = QoFireResult()
+    lib().qo_fire_minimize(_p(h), h.size, C.byref(p), C.byref(noise.s), C.byref(fp), C.byref(res))
+    return res

@@ -3,8 +3,9 @@
  *
  * Plain-C FP64 restatement of the reference algorithm (IMTEK-Simulation/qEW,
  * src/filtered_noise.h, src/filtered_noise.cpp, src/qew_model.h, src/lbfgs.h,
- * src/dynamics.h, src/rosso_krauth.h). Only the tests, the smoke check and the
- * benchmark's CPU-baseline leg load this code, and only as the checker.
+ * src/dynamics.h, src/rosso_krauth.h, src/fire.h; the seeded field's
+ * std::mt19937_64 draws). Only the tests, the smoke check and the benchmark's
+ * CPU-baseline leg load this code, and only as the checker.
  *
  * Compile with -ffp-contract=off: the reference is built as ISO C++20 (no GNU
  * extensions), where GCC does not contract a*b+c into an FMA, so expression-
@@ -542,6 +543,68 @@ static void qo_gradient_impl(const double *h, int n, const qo_params *p,
 void qo_gradient(const double *h, int n, const qo_params *p,
                  const qo_noise *nz, double *grad) {
     qo_gradient_impl(h, n, p, nz, grad, 0);
+}
+
+/* fire_minimize, fire.h:41-131: v += dt F; P = F.v; adapt dt / alpha; mix v
+ * toward F; h += dt v; F refreshed. Serial sums in index order. */
+void qo_fire_minimize(double *h, int n, const qo_params *p, const qo_noise *nz,
+                      const qo_fire_params *fp, qo_fire_result *res) {
+    double *g = (double *)malloc(sizeof(double) * 2 * (size_t)n);
+    double *v = g + n;
+    for (int i = 0; i < n; ++i) v[i] = 0.0;
+    double dt = (fp->dt_init > 0) ? fp->dt_init : 0.1 * fp->dt_max;
+    double alpha = fp->alpha_start;
+    int n_pos = 0;
+    qo_gradient(h, n, p, nz, g);
+    for (int it = 0; it < fp->max_iter; ++it) {
+        double m = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double a = fabs(g[i]);
+            if (a > m) m = a;
+        }
+        if (m < fp->ftol) {
+            res->iterations = it;
+            res->max_force = m;
+            res->converged = 1;
+            free(g);
+            return;
+        }
+        for (int i = 0; i < n; ++i) v[i] -= dt * g[i];
+        double P = 0.0;
+        for (int i = 0; i < n; ++i) P += -g[i] * v[i];
+        if (P > 0) {
+            if (n_pos > fp->n_min) {
+                dt = fmin(dt * fp->f_inc, fp->dt_max);
+                alpha *= fp->f_alpha;
+            }
+            ++n_pos;
+        } else {
+            for (int i = 0; i < n; ++i) v[i] = 0.0;
+            dt *= fp->f_dec;
+            alpha = fp->alpha_start;
+            n_pos = 0;
+        }
+        double nv2 = 0.0, nf2 = 0.0;
+        for (int i = 0; i < n; ++i) nv2 += v[i] * v[i];
+        for (int i = 0; i < n; ++i) nf2 += g[i] * g[i];
+        const double nf = sqrt(nf2);
+        if (nf > 0) {
+            const double a = alpha;
+            const double scale = alpha * sqrt(nv2) / nf;
+            for (int i = 0; i < n; ++i) v[i] = (1.0 - a) * v[i] - scale * g[i];
+        }
+        for (int i = 0; i < n; ++i) h[i] += dt * v[i];
+        qo_gradient(h, n, p, nz, g);
+    }
+    double m = 0.0;
+    for (int i = 0; i < n; ++i) {
+        const double a = fabs(g[i]);
+        if (a > m) m = a;
+    }
+    res->iterations = fp->max_iter;
+    res->max_force = m;
+    res->converged = 0;
+    free(g);
 }
 
 void qo_gradient_omp(const double *h, int n, const qo_params *p,

@@ -83,6 +83,18 @@ typedef struct { /* RkResult, rosso_krauth.h:43-49 */
     double total_advance, mean_h;
 } qo_rk_result;
 
+typedef struct { /* FireParams, fire.h:21-31 */
+    double dt_max, dt_init, ftol;
+    int max_iter, n_min;
+    double f_inc, f_dec, alpha_start, f_alpha;
+} qo_fire_params;
+
+typedef struct { /* FireResult, fire.h:33-37 */
+    int iterations;
+    double max_force;
+    int converged;
+} qo_fire_result;
+
 /* ---- B-spline field (filtered_noise.h / filtered_noise.cpp) ---- */
 void qo_bspline_weights_value(double t, double w[4]);
 void qo_bspline_weights(double t, double w[4], double dw[4]);
@@ -116,6 +128,9 @@ double qo_objective_trial(const double *x0, const double *d, double alpha,
                           int n, const qo_params *p, const qo_noise *nz);
 void qo_gradient(const double *h, int n, const qo_params *p,
                  const qo_noise *nz, double *grad);
+/* fire_minimize, fire.h:41-131 (serial) */
+void qo_fire_minimize(double *h, int n, const qo_params *p, const qo_noise *nz,
+                      const qo_fire_params *fp, qo_fire_result *res);
 /* Thread-parallel gradient/objective (OpenMP): the timed CPU baseline. */
 void qo_gradient_omp(const double *h, int n, const qo_params *p,
                      const qo_noise *nz, double *grad);

@@ -19,6 +19,7 @@ test stubs (ZeroNoise, HarmonicWell, ...)  :func:`ZeroNoise` etc.
 ``lbfgs_minimize(h, p, noise, lp)``        :func:`lbfgs_minimize`
 ``LangevinDynamics(n, seed).step(...)``    :class:`LangevinDynamics`
 ``rk_site_velocity`` / ``rk_block``        :func:`rk_site_velocity`, :func:`rk_block`
+``fire_minimize(h, p, noise, fp)``         :func:`fire_minimize`
 ``static_sweep`` / ``dynamic_anneal`` /    :func:`static_sweep`, :func:`dynamic_anneal`,
 ``depinning_ramp`` (qew_runs.h)            :func:`depinning_ramp`
 =========================================  ====================================
@@ -51,7 +52,7 @@ __all__ = [
     "depinning_bisect", "Context", "default_context", "QewError", "Server",
     "StaticConfig", "StaticProfile", "static_sweep", "DynamicConfig", "DynamicSnapshot",
     "DynamicResult", "dynamic_anneal", "DepinningConfig", "DepinningStep", "DepinningResult",
-    "depinning_ramp",
+    "depinning_ramp", "FireParams", "FireResult", "fire_minimize", "line_statistics",
 ]
 
 
@@ -633,6 +634,65 @@ def depinning_bisect(h, p: Params, noise: _Noise, rp: RkParams, f_lo: float, f_h
         float(rtol), int(max_steps), int(precision), C.byref(fc), C.byref(flo), C.byref(fhi),
         C.byref(nb)), ctx.h, "depinning_bisect")
     return fc.value, flo.value, fhi.value, nb.value
+
+
+# ------------------------------------------------------------------- FIRE
+@dataclass
+class FireParams:  # fire.h:21-31
+    dt_max: float = 0.0  # required, > 0
+    dt_init: float = 0.0
+    ftol: float = 1e-6
+    max_iter: int = 100000
+    n_min: int = 5
+    f_inc: float = 1.1
+    f_dec: float = 0.5
+    alpha_start: float = 0.1
+    f_alpha: float = 0.99
+
+    def c(self) -> _capi.qew_fire_params:
+        return _capi.qew_fire_params(float(self.dt_max), float(self.dt_init), float(self.ftol),
+                                     int(self.max_iter), int(self.n_min), float(self.f_inc),
+                                     float(self.f_dec), float(self.alpha_start),
+                                     float(self.f_alpha))
+
+
+@dataclass
+class FireResult:  # fire.h:33-37
+    iterations: int = 0
+    max_force: float = 0.0
+    converged: bool = False
+
+
+def fire_minimize(h, p: Params, noise: _Noise, fp: FireParams) -> FireResult:
+    """fire_minimize(h, p, noise, fp), fire.h:41-131: relaxes h in place."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    pc, fc, res = p.c(), fp.c(), _capi.qew_fire_result()
+    _capi.check(ctx.lib.qew_fire_minimize(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
+                                          C.byref(fc), C.byref(res)), ctx.h, "fire_minimize")
+    return FireResult(res.iterations, res.max_force, bool(res.converged))
+
+
+# ------------------------------------------------------------- statistics
+def line_statistics(h, physical_size: float, ctx: Context | None = None):
+    """(ell, acf, q, psd) of periodic lines h[n] or h[count, n] (CUDA float64),
+    with the definitions of qew_line_statistics in include/qew_gpu.h."""
+    torch = _torch()
+    ctx = ctx or default_context()
+    ctx.sync_stream()
+    h2 = h.reshape(1, -1) if h.dim() == 1 else h
+    h2 = h2.contiguous()
+    count, n = h2.shape
+    nh = n // 2 + 1
+    kw = dict(dtype=torch.float64, device=h2.device)
+    ell, q = torch.empty(nh, **kw), torch.empty(nh, **kw)
+    acf, psd = torch.empty((count, nh), **kw), torch.empty((count, nh), **kw)
+    _capi.check(ctx.lib.qew_line_statistics(ctx.h, count, _ptr(h2), n, float(physical_size),
+                                            _ptr(ell), _ptr(acf), _ptr(q), _ptr(psd)),
+                ctx.h, "line_statistics")
+    if h.dim() == 1:
+        acf, psd = acf[0], psd[0]
+    return ell, acf, q, psd
 
 
 # ---------------------------------------------------------------- drivers

@@ -61,6 +61,15 @@ class qew_rk_result(C.Structure):
                 ("mean_h", D)]
 
 
+class qew_fire_params(C.Structure):
+    _fields_ = [("dt_max", D), ("dt_init", D), ("ftol", D), ("max_iter", I), ("n_min", I),
+                ("f_inc", D), ("f_dec", D), ("alpha_start", D), ("f_alpha", D)]
+
+
+class qew_fire_result(C.Structure):
+    _fields_ = [("iterations", I), ("max_force", D), ("converged", I)]
+
+
 class qew_ensemble_line(C.Structure):
     _fields_ = [("field", VP), ("d_h", VP), ("n", I), ("p", qew_params), ("precond_shift", D)]
 
@@ -193,6 +202,11 @@ _SIGS = {
     "qew_depinning_bisect_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params),
                                       C.POINTER(qew_rk_params), D, D, D, I, I, PD, PD, PD,
                                       C.POINTER(I)]),
+    "qew_fire_default_params": (I, [C.POINTER(qew_fire_params)]),
+    "qew_fire_minimize": (I, [VP, VP, VP, I, C.POINTER(qew_params), C.POINTER(qew_fire_params),
+                              C.POINTER(qew_fire_result)]),
+    "qew_line_statistics": (I, [VP, I, VP, I, D, VP, VP, VP, VP]),
+    "qew_line_statistics_host": (I, [VP, I, VP, I, D, VP, VP, VP, VP]),
     # drivers (qew_runs.h)
     "qew_static_config_default": (None, [C.POINTER(qew_static_config)]),
     "qew_static_sweep": (I, [VP, VP, C.POINTER(qew_static_config),

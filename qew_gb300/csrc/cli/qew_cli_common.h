@@ -57,6 +57,20 @@ class Gpu {
     qew_field *field = nullptr;
 };
 
+// ell, acf, q, psd of one host profile (qew_line_statistics_host).
+inline LineStats line_stats(Gpu &gpu, const std::vector<double> &h, double L) {
+    const int n = (int)h.size(), nh = n / 2 + 1;
+    LineStats s;
+    s.ell.resize(nh);
+    s.acf.resize(nh);
+    s.q.resize(nh);
+    s.psd.resize(nh);
+    gpu.check(qew_line_statistics_host(gpu.ctx, 1, h.data(), n, L, s.ell.data(), s.acf.data(),
+                                       s.q.data(), s.psd.data()),
+              "line_statistics");
+    return s;
+}
+
 // main() body: run(argc, argv) with the exit-code convention.
 template <class F>
 int guarded_main(const char *prog, const char *usage, F run, int argc, char **argv) {

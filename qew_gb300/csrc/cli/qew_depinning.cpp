@@ -2,7 +2,8 @@
 // reference's depinning run (executables/qew_depinning/main.cpp) with the
 // same options, defaults (RK knobs derived from Ly/ny), console lines and
 // output keys, on the GPU. Added options: --bisect_rtol (bisect f_c after
-// the ramp; adds the key f_c), --precision fp64|fp32split, --device.
+// the ramp; adds the key f_c), --precision fp64|fp32split, --analysis 1 (ell,
+// acf, q, psd beside each blocked profile), --device.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -29,6 +30,7 @@ const char *kUsage =
     "  --dstep --max_advance --runaway --root_tol --sweep_tol --max_sweeps\n"
     "  --bisect_rtol     bisect f_c to this relative width after the ramp (default 0: off)\n"
     "  --precision       fp64|fp32split         (default fp64)\n"
+    "  --analysis        1: add ell, acf, q, psd beside each blocked profile (default 0)\n"
     "  --device          CUDA device            (default 0)\n";
 
 struct Collect {
@@ -71,6 +73,7 @@ int run(int argc, char **argv) {
     const std::string fname = a.text("output", "depinning_" + model + default_suffix());
     cfg.bisect_rtol = a.real("bisect_rtol", 0.0);
     cfg.precision = cli::parse_precision(a.text("precision", "fp64"));
+    const bool analysis = a.integer("analysis", 0) != 0;
     const int device = a.integer("device", 0);
     a.finish();
     std::unique_ptr<Sink> sink = open_sink(fname);
@@ -94,6 +97,13 @@ int run(int argc, char **argv) {
     if (res.f_c >= 0)
         std::printf("f_c=%.10g  bracket [%.10g, %.10g]  %d bisection blocks\n", res.f_c,
                     res.f_c_lo, res.f_c_hi, res.bisect_blocks);
+    std::vector<LineStats> stats(col.steps.size());
+    if (analysis)
+        for (size_t k = 0; k < col.steps.size(); ++k)
+            if (col.steps[k].blocked) {
+                stats[k] = cli::line_stats(gpu, col.steps[k].h, cfg.Lx);
+                col.steps[k].stats = &stats[k];
+            }
     write_depinning(*sink, cfg, res, col.steps);
     sink->close();
     std::printf("wrote %s\n", fname.c_str());

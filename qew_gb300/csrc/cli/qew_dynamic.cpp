@@ -1,7 +1,8 @@
 // qew_dynamic -- annealed overdamped Langevin dynamics, the executable of the
 // reference's dynamic run (executables/qew_dynamic/main.cpp) with the same
 // options, defaults, console lines and output keys, on the GPU. Added
-// options: --dt (explicit timestep), --precision fp64|fp32split, --device.
+// options: --dt (explicit timestep), --precision fp64|fp32split, --analysis 1
+// (ell, acf, q, psd beside each snapshot), --device.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -29,6 +30,7 @@ const char *kUsage =
     "  --output          output file            (default dynamic_<model>.npz, .h5 with HDF5)\n"
     "  --dt              timestep               (default: from xi and the thermal lengths)\n"
     "  --precision       fp64|fp32split         (default fp64)\n"
+    "  --analysis        1: add ell, acf, q, psd beside each snapshot (default 0)\n"
     "  --device          CUDA device            (default 0)\n";
 
 struct Collect {
@@ -64,6 +66,7 @@ int run(int argc, char **argv) {
     const std::string fname = a.text("output", "dynamic_" + model + default_suffix());
     cfg.dt = a.real("dt", 0.0);
     cfg.precision = cli::parse_precision(a.text("precision", "fp64"));
+    const bool analysis = a.integer("analysis", 0) != 0;
     const int device = a.integer("device", 0);
     a.finish();
     std::unique_ptr<Sink> sink = open_sink(fname);
@@ -79,6 +82,12 @@ int run(int argc, char **argv) {
     std::printf("dt=%.3g  total_time=%.3g  steps=%ld  line_tension=%.4g\n", res.dt, res.total_time,
                 (long)(res.total_time / res.dt), res.line_tension);
     for (const SnapshotOut &s : col.snaps) std::printf("  saved t=%.6g\n", s.t);
+    std::vector<LineStats> stats(col.snaps.size());
+    if (analysis)
+        for (size_t k = 0; k < col.snaps.size(); ++k) {
+            stats[k] = cli::line_stats(gpu, col.snaps[k].h, cfg.Lx);
+            col.snaps[k].stats = &stats[k];
+        }
     write_dynamic(*sink, cfg, res.line_tension, col.snaps);
     sink->close();
     std::printf("wrote %s\n", fname.c_str());

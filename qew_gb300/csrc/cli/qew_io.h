@@ -246,9 +246,25 @@ inline std::unique_ptr<Sink> open_sink(const std::string &fname) {
 }
 
 // ------------------------------------------------------------ the writers
+// Roughness statistics written beside a profile (the datasets the reference's
+// post-processing adds to every ".../h" group: ell, acf, q, psd;
+// tools/postprocess_static.py:38-46), when the executable is asked for them.
+struct LineStats {
+    std::vector<double> ell, acf, q, psd;
+};
+
+inline void write_line_stats(Sink &s, const std::string &prefix, const LineStats *st) {
+    if (!st) return;
+    s.vector(prefix + "/ell", st->ell);
+    s.vector(prefix + "/acf", st->acf);
+    s.vector(prefix + "/q", st->q);
+    s.vector(prefix + "/psd", st->psd);
+}
+
 struct StaticOut {
     double pinning_length_over_xi;
     std::vector<double> h;
+    const LineStats *stats = nullptr;
 };
 
 // write_static, qew_io.h:24-34.
@@ -259,12 +275,14 @@ inline void write_static(Sink &s, const qew_static_config &c, const std::vector<
                                    "/pinning_length=" + fmt("%.3g", p.pinning_length_over_xi);
         s.scalar(prefix + "/pinning_length", p.pinning_length_over_xi);
         s.vector(prefix + "/h", p.h);
+        write_line_stats(s, prefix, p.stats);
     }
 }
 
 struct SnapshotOut {
     double t;
     std::vector<double> h;
+    const LineStats *stats = nullptr;
 };
 
 // write_dynamic, qew_io.h:36-48.
@@ -277,6 +295,7 @@ inline void write_dynamic(Sink &s, const qew_dynamic_config &c, double line_tens
                                    fmt("%.3g", line_tension);
         s.scalar(prefix + "/pinning_length", c.pinning_length_over_xi);
         s.vector(prefix + "/h", sn.h);
+        write_line_stats(s, prefix, sn.stats);
     }
 }
 
@@ -284,6 +303,7 @@ struct DepinningOut {
     double f;
     bool blocked;
     std::vector<double> h;  // blocked steps only
+    const LineStats *stats = nullptr;
 };
 
 // write_depinning, qew_io.h:50-63; f_c (bisection) is an added key, written
@@ -296,6 +316,7 @@ inline void write_depinning(Sink &s, const qew_depinning_config &c, const qew_de
         const std::string prefix = "driving_force=" + fmt("%.4g", st.f);
         s.vector(prefix + "/h", st.h);
         s.scalar(prefix + "/pinning_length", c.pinning_length_over_xi);
+        write_line_stats(s, prefix, st.stats);
     }
     if (r.f_c_upper_bound >= 0) s.scalar("f_c_upper_bound", r.f_c_upper_bound);
     if (r.f_c >= 0) s.scalar("f_c", r.f_c);

@@ -1,7 +1,9 @@
 // qew_static -- L-BFGS relaxation of a flat line at each pinning length, the
 // executable of the reference's static run (executables/qew_static/main.cpp)
 // with the same options, defaults, console lines and output keys, on the GPU.
-// Added options: --lbfgs_m (history size), --device.
+// Added options: --lbfgs_m (history size), --analysis 1 (write ell, acf, q,
+// psd beside each profile, as the reference's post-processing does),
+// --device.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -26,6 +28,7 @@ const char *kUsage =
     "  --seed            noise RNG seed         (default 1)\n"
     "  --output          output file            (default static_<model>.npz, .h5 with HDF5)\n"
     "  --lbfgs_m         L-BFGS history size    (default 8)\n"
+    "  --analysis        1: add ell, acf, q, psd beside each profile (default 0)\n"
     "  --device          CUDA device            (default 0)\n";
 
 int run(int argc, char **argv) {
@@ -54,6 +57,7 @@ int run(int argc, char **argv) {
     const uint64_t seed = a.u64("seed", 1);
     const std::string fname = a.text("output", "static_" + model + default_suffix());
     cfg.lbfgs_m = a.integer("lbfgs_m", 8);
+    const bool analysis = a.integer("analysis", 0) != 0;
     const int device = a.integer("device", 0);
     a.finish();
     std::unique_ptr<Sink> sink = open_sink(fname);
@@ -65,6 +69,7 @@ int run(int argc, char **argv) {
     gpu.check(qew_static_sweep(gpu.ctx, gpu.field, &cfg, prof.data(), h.data()), "static_sweep");
 
     std::vector<StaticOut> out;
+    std::vector<LineStats> stats(prof.size());
     for (size_t k = 0; k < prof.size(); ++k) {
         const qew_static_profile &p = prof[k];
         std::printf("lp/xi=%-6.3g lt=%-10.4g iters=%-7d max|F|=%.3e  %s\n",
@@ -73,6 +78,10 @@ int run(int argc, char **argv) {
         out.push_back(StaticOut{p.pinning_length_over_xi,
                                 std::vector<double>(h.begin() + k * cfg.nx,
                                                     h.begin() + (k + 1) * cfg.nx)});
+        if (analysis) {
+            stats[k] = cli::line_stats(gpu, out.back().h, cfg.Lx);
+            out.back().stats = &stats[k];
+        }
     }
     write_static(*sink, cfg, out);
     sink->close();

@@ -34,6 +34,10 @@ struct qew_ctx {
     void *scratch = nullptr;
     size_t scratch_bytes = 0;
     uint64_t launches = 0;
+    // upper bound on the warps of this context's persistent (cooperative)
+    // kernels; 0 = every resident slot of the GPU. Contexts that share the GPU
+    // (the server's workers) take a share each.
+    int warp_cap = 0;
     std::string last_error;
     // copy streams and slot events of the host-buffer batch pipeline
     // (created on first use)

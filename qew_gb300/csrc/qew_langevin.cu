@@ -264,7 +264,9 @@ qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h
         int per_sm = 0;
         QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRunBS, 0));
         const int want = (n + kRunTile - 1) / kRunTile;
-        const int grid = std::max(1, std::min(want, ctx->num_sms * std::max(per_sm, 1)));
+        int slots = ctx->num_sms * std::max(per_sm, 1);
+        if (ctx->warp_cap > 0) slots = std::min(slots, std::max(1, ctx->warp_cap / (kRunBS / 32)));
+        const int grid = std::max(1, std::min(want, slots));
         void *args[] = {(void *)&nz, (void *)&d_h, (void *)&tmp, (void *)&n, (void *)&L,
                         (void *)&lt, (void *)&fd, (void *)&model, (void *)&steps,
                         (void *)&d_drift, (void *)&d_diff, (void *)&d_rs, (void *)&seed,

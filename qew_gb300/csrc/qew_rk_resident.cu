@@ -24,8 +24,10 @@
 namespace {
 
 constexpr int kRkBS = 32;  // one warp per CTA: a 16384-site line still spreads over every SM
-constexpr int kRkGroup = 8;  // lanes per site: 7 march points or 3 bisection levels per round
-template <class Noise>
+// kRkGroup lanes per site (8: 7 march points or 3 bisection levels per round;
+// 1: the serial search). All sizes give the same result; the launch takes the
+// largest whose grid fits the GPU (or the context's share of it).
+template <class Noise, int kRkGroup>
 __global__ void __launch_bounds__(kRkBS)
 k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n, double dx,
               double lt, double f, int model, RkP rp, double *partials, GridSync *sync,
@@ -60,10 +62,16 @@ k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n,
                 const int ip = (i + 1 == n) ? 0 : i + 1;
                 bool found = false;
                 const double hi = __ldcg(h + i);
-                const double hnew = rk_forward_zero_group<kRkGroup>(
-                    nz, i, n, dx, lt, f, model, hi, __ldcg(h + im), __ldcg(h + ip), rp, found,
-                    glane, gmask);
-                __syncwarp(gmask);  // every lane has read h[i]
+                double hnew;
+                if constexpr (kRkGroup == 1) {
+                    hnew = rk_forward_zero(nz, i, n, dx, lt, f, model, hi, __ldcg(h + im),
+                                           __ldcg(h + ip), rp, found);
+                } else {
+                    hnew = rk_forward_zero_group<kRkGroup>(nz, i, n, dx, lt, f, model, hi,
+                                                          __ldcg(h + im), __ldcg(h + ip), rp,
+                                                          found, glane, gmask);
+                    __syncwarp(gmask);  // every lane has read h[i]
+                }
                 if (glane == 0) {
                     const double a = hnew - hi;
                     adv[i] = a;
@@ -106,12 +114,28 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
                                  qew_rk_result *res) {
     const double dx = p->physical_size / (double)n;
     const RkP rk = rkp_from(rp);
-    int max_per_sm = 0;
     auto launch = [&](auto nz) -> qew_status {
-        auto kern = k_rk_resident<decltype(nz)>;
-        QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_per_sm, kern, kRkBS, 0));
-        const int want = (int)(((long long)(n / 2) * kRkGroup + kRkBS - 1) / kRkBS);
-        const int grid = std::max(1, std::min(want, ctx->num_sms * std::max(max_per_sm, 1)));
+        using N = decltype(nz);
+        // the widest group whose grid fits the resident CTA slots (or the
+        // context's share of them); the serial form takes what is left
+        const void *forms[4] = {(const void *)k_rk_resident<N, 8>, (const void *)k_rk_resident<N, 4>,
+                                (const void *)k_rk_resident<N, 2>, (const void *)k_rk_resident<N, 1>};
+        const int sizes[4] = {8, 4, 2, 1};
+        const long long half = n / 2;
+        const void *kern = nullptr;
+        int grid = 1;
+        for (int k = 0; k < 4; ++k) {
+            int per_sm = 0;
+            QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forms[k], kRkBS, 0));
+            int slots = ctx->num_sms * std::max(per_sm, 1);
+            if (ctx->warp_cap > 0) slots = std::min(slots, ctx->warp_cap / (kRkBS / 32));
+            const long long want = (half * sizes[k] + kRkBS - 1) / kRkBS;
+            if (want <= slots || k == 3) {
+                kern = forms[k];
+                grid = (int)std::max(1LL, std::min(want, (long long)slots));
+                break;
+            }
+        }
         // scratch: adv[n], partials[3*grid], sync word, result
         const size_t off_part = ((size_t)n * sizeof(double) + 255) & ~size_t(255);
         const size_t off_sync = (off_part + 3 * (size_t)grid * sizeof(double) + 255) & ~size_t(255);
@@ -129,8 +153,8 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
         void *args[] = {(void *)&nz, (void *)&d_h, (void *)&adv, (void *)&n, (void *)&dx,
                         (void *)&lt, (void *)&fd, (void *)&model, (void *)&rk, (void *)&part,
                         (void *)&sync, (void *)&d_res};
-        QEW_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kRkBS), args,
-                                                  0, ctx->stream));
+        QEW_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kRkBS), args, 0,
+                                                  ctx->stream));
         QEW_TRY(qew_launch_check(ctx, "rk_resident"));
         GridSync hs;
         QEW_CUDA(ctx, cudaMemcpyAsync(res, d_res, sizeof(qew_rk_result), cudaMemcpyDeviceToHost,

@@ -164,7 +164,13 @@ void worker_main(qew_server *s) {
     cudaStream_t stream = nullptr;
     const bool ok = qew_ctx_create(s->device, &ctx) == QEW_OK &&
                     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) == cudaSuccess;
-    if (ok) qew_ctx_set_stream(ctx, stream);
+    if (ok) {
+        qew_ctx_set_stream(ctx, stream);
+        // persistent kernels of concurrent requests share the SMs: each worker's
+        // cooperative grids take at most its share of the GPU's warp slots (64
+        // per SM), never less than four warps per SM
+        ctx->warp_cap = std::max(4 * ctx->num_sms, 64 * ctx->num_sms / s->max_inflight);
+    }
     for (;;) {
         qew_server::Job job;
         {

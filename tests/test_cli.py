@@ -123,3 +123,29 @@ def test_executables_help_and_usage_errors(name):
         r = subprocess.run([exe, *bad], capture_output=True, text=True, timeout=60)
         assert r.returncode == 2, (bad, r.stderr)
         assert r.stderr.startswith(name + ": ") and "--model" in r.stderr  # message + usage
+
+
+def build_hpp_probe(out_dir):
+    """Compile tests/native/hpp_probe.cpp against include/qew_gpu.hpp and the
+    built library (host compiler + CUDA runtime for the caller's buffers)."""
+    from qew_gb300 import build
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    if not os.path.exists(build.LIB):
+        pytest.skip("library not built")
+    cuda = build._cuda_home()
+    out = os.path.join(str(out_dir), "hpp_probe")
+    subprocess.run([cxx, "-std=c++17", "-O1", "-Wall", "-I" + os.path.join(ROOT, "include"),
+                    "-I" + os.path.join(cuda, "include"),
+                    os.path.join(ROOT, "tests", "native", "hpp_probe.cpp"), "-o", out,
+                    "-L" + build.OUT_DIR, "-lqew_gb300", "-Wl,-rpath," + build.OUT_DIR,
+                    "-L" + os.path.join(cuda, "lib64"), "-lcudart",
+                    "-Wl,-rpath," + os.path.join(cuda, "lib64")], check=True)
+    return out
+
+
+def test_cpp_face_compiles_and_links(tmp_path):
+    """include/qew_gpu.hpp: the reference's signatures over the C ABI build
+    against the library (it runs in tests/test_gpu_runs.py)."""
+    assert os.path.exists(build_hpp_probe(tmp_path))

@@ -221,3 +221,29 @@ def test_executable_dynamic_and_depinning(Q, tmp_path):
     assert "driving_force=0/h" in z.files and "f_c_upper_bound" in z.files and "f_c" in z.files
     fc_ub = float(z["f_c_upper_bound"])
     assert fc_ub - 2.0 <= float(z["f_c"]) <= fc_ub
+
+
+def test_executable_analysis_keys(Q, tmp_path):
+    """--analysis 1 adds ell, acf, q, psd beside every profile (the datasets of
+    the reference's post-processing), equal to line_statistics of that profile."""
+    import torch
+    _run("qew_static", "--model", "linear", "--nx", "128", "--ny", "32", "--Lx", "4",
+         "--pinning_lengths", "2", "--analysis", "1", "--output", "s.npz", cwd=tmp_path)
+    z = np.load(tmp_path / "s.npz")
+    pre = "driving_force=0/pinning_length=2"
+    for key in ("ell", "acf", "q", "psd"):
+        assert z[pre + "/" + key].shape == (65,)
+    ell, acf, q, psd = (t.cpu().numpy() for t in Q.line_statistics(
+        torch.as_tensor(z[pre + "/h"], device="cuda"), 4.0))
+    assert np.array_equal(z[pre + "/acf"], acf) and np.array_equal(z[pre + "/psd"], psd)
+    assert np.array_equal(z[pre + "/ell"], ell) and np.array_equal(z[pre + "/q"], q)
+
+
+def test_cpp_face_runs(Q, tmp_path):
+    """The C++ face (include/qew_gpu.hpp) used as a reference caller would:
+    solvers, drivers, std::invalid_argument on odd n, Error statuses."""
+    from test_cli import build_hpp_probe
+    exe = build_hpp_probe(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "FAIL" not in r.stdout and r.stdout.count("ok ") == 8

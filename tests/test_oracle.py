@@ -211,3 +211,22 @@ def test_philox_normals_moments(O):
     a, b = O.philox_normals(7, 3, 1000), O.philox_normals(7, 3, 1000)
     assert np.array_equal(a, b)
     assert not np.array_equal(a, O.philox_normals(7, 4, 1000))
+
+
+def test_oracle_fire_reference_cases(O):
+    """The reference's FIRE known answers (tests/test_fire.cpp) on the oracle."""
+    import math
+    n = 128
+    h = 0.5 + 0.3 * np.cos(4 * np.pi * np.arange(n) / n)
+    r = O.fire_minimize(h, O.params(float(n), 1.0, 0.0, 0), O.ZeroNoise(),
+                        O.fire_params(0.1, ftol=1e-9))
+    assert r.converged and r.max_force < 1e-9 and np.ptp(h) < 1e-6
+    n = 96
+    h = np.zeros(n)
+    r = O.fire_minimize(h, O.params(float(n), 1.0, 0.0, 0), O.HarmonicWell(2.0, 0.5),
+                        O.fire_params(0.1 * math.sqrt(1.0), ftol=1e-9))
+    assert r.converged and np.max(np.abs(h - 0.5)) < 1e-6
+    h = np.zeros(64)
+    r = O.fire_minimize(h, O.params(64.0, 1.0, 0.0, 0), O.HarmonicWell(2.0, 0.5),
+                        O.fire_params(0.1, ftol=1e-12, max_iter=3))
+    assert not r.converged and r.iterations == 3
