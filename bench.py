@@ -319,6 +319,34 @@ def run_static(args, Q, torch):
     out["value"] = 3.0 / gpu_total
     out["cpu_solves_per_s"] = 3.0 / cpu_total
     out["cpu"] = {"cores": 1, "kind": "port", "sample": "the three solves, serial oracle"}
+    # The reference's published end-to-end L-BFGS case (3.55 s, 2470 iterations,
+    # Kokkos Serial): qew_static's defaults (seeded FilteredNoise 4096 x 512,
+    # Lx = 32, xi = 0.1, arclength) at lambda_p/xi = 1 (Gamma = 1), m = 8,
+    # preconditioned, ftol 1e-6, through static_sweep.
+    fld = Q.FilteredNoise.seeded(4096, 512, 32.0, 1.0, 1.0, 0.1, 0.1, 1)
+    cfg = Q.StaticConfig(model=Q.Model.Arclength, nx=4096, ny=512, Lx=32.0, Ly=1.0, xi=0.1,
+                         pinning_lengths_over_xi=(1.0,), ftol=1e-6, max_iter=20000)
+    Q.static_sweep(cfg, fld)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prof = Q.static_sweep(cfg, fld)[0]
+    tg = time.perf_counter() - t0
+    of = O.BSplineField(np.zeros((4096, 512)), 32.0, 1.0, coef=fld.coefficients())
+    hc = np.full(4096, 0.5)
+    olp = O.lbfgs_default_params(m=8, ftol=1e-6, max_iter=20000, precondition=1,
+                                 precond_shift=0.5 * (32.0 / 4096) * 1.0 / 0.01)
+    t0 = time.perf_counter()
+    rc = O.lbfgs_minimize(hc, O.params(32.0, 1.0, 0.0, 1), of, olp)
+    tc = time.perf_counter() - t0
+    out["reference_case"] = {
+        "workload": "qew_static defaults at lambda_p/xi=1: n=4096, 4096x512 seeded field, "
+                    "Lx=32, xi=0.1, arclength, m=8, preconditioned, ftol 1e-6",
+        "gpu_s": tg, "gpu_iterations": prof.result.iterations,
+        "gpu_converged": bool(prof.result.converged), "cpu_oracle_s": tc,
+        "cpu_oracle_iterations": rc.iterations, "cpu_oracle_converged": bool(rc.converged),
+        "max_abs_h_diff": float(np.max(np.abs(prof.h - hc))),
+        "published_reference_s": 3.55, "published_reference_iterations": 2470,
+        "published_reference_hardware": "Kokkos Serial, one CPU core (docs/fix_plan.md)"}
     return out
 
 

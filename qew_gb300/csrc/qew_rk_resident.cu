@@ -24,9 +24,12 @@
 namespace {
 
 constexpr int kRkBS = 32;  // one warp per CTA: a 16384-site line still spreads over every SM
+#ifndef QEW_RK_WARPS_PER_SM
+#define QEW_RK_WARPS_PER_SM 4  // build-time tuning knob (measured on GB300)
+#endif
 // kRkGroup lanes per site (8: 7 march points or 3 bisection levels per round;
-// 1: the serial search). All sizes give the same result; the launch takes the
-// largest whose grid fits the GPU (or the context's share of it).
+// 4: 3 points or 2 levels; 1: the serial search). All sizes give the same
+// result; the launch picks one by the budget below.
 template <class Noise, int kRkGroup>
 __global__ void __launch_bounds__(kRkBS)
 k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n, double dx,
@@ -116,21 +119,28 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
     const RkP rk = rkp_from(rp);
     auto launch = [&](auto nz) -> qew_status {
         using N = decltype(nz);
-        // the widest group whose grid fits the resident CTA slots (or the
-        // context's share of them); the serial form takes what is left
-        const void *forms[4] = {(const void *)k_rk_resident<N, 8>, (const void *)k_rk_resident<N, 4>,
-                                (const void *)k_rk_resident<N, 2>, (const void *)k_rk_resident<N, 1>};
-        const int sizes[4] = {8, 4, 2, 1};
+        // the widest group whose grid stays within QEW_RK_WARPS_PER_SM warps per
+        // SM (and the resident slots, or the context's share of them): wider
+        // groups shorten each site's chain of dependent evaluations but
+        // multiply its FP64 work, which pays only while the SMs' FP64 pipes
+        // idle; the serial form takes what is left
+        // (a 2-lane group would evaluate one bisection level per round, like
+        // the serial search, at twice the work: never worth it)
+        const void *forms[3] = {(const void *)k_rk_resident<N, 8>, (const void *)k_rk_resident<N, 4>,
+                                (const void *)k_rk_resident<N, 1>};
+        const int sizes[3] = {8, 4, 1};
         const long long half = n / 2;
         const void *kern = nullptr;
         int grid = 1;
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < 3; ++k) {
             int per_sm = 0;
             QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forms[k], kRkBS, 0));
             int slots = ctx->num_sms * std::max(per_sm, 1);
             if (ctx->warp_cap > 0) slots = std::min(slots, ctx->warp_cap / (kRkBS / 32));
+            const long long budget =
+                std::min<long long>(slots, (long long)QEW_RK_WARPS_PER_SM * ctx->num_sms);
             const long long want = (half * sizes[k] + kRkBS - 1) / kRkBS;
-            if (want <= slots || k == 3) {
+            if (want <= budget || k == 2) {
                 kern = forms[k];
                 grid = (int)std::max(1LL, std::min(want, (long long)slots));
                 break;
