@@ -3,7 +3,7 @@
 // ensemble kernel.
 #pragma once
 
-#include "qew_block.cuh"
+#include "qew_team.cuh"
 
 constexpr int kLbfgsMaxM = 32;
 constexpr int kLbfgsVecs = 6;  // g, g_new, d, q, edge dV/dy, edge slope
@@ -60,14 +60,14 @@ struct LbfgsShared {
 
 // Workspace (npad-strided vectors): g, g_new, d, q, ev, es, then 2(m+1)
 // history buffers (m S rows + spare, m Y rows + spare).
-template <class Noise, int BS>
-__device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h, const int n,
-                            const qew_params P, const LbfgsCfg cfg, const PrecondCoef pc,
-                            double *ws, size_t npad) {
-    __shared__ double s_w[96];
-    __shared__ double s_b[BS];
+template <class Noise, class Team>
+__device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restrict__ h,
+                                       const int n, const qew_params P, const LbfgsCfg cfg,
+                                       const PrecondCoef pc, double *ws, size_t npad) {
+    __shared__ double s_b[Team::kBS];
+    __shared__ double s_agg[2 * kTeamMaxCtas];
     __shared__ LbfgsShared sh;
-    const int t = threadIdx.x;
+    const int t0 = T.tid(), ts = T.stride();
     const LineDx dx = make_line_dx(P.physical_size, n);
     const double lt = P.line_tension, f = P.driving_force;
     const int model = P.model;
@@ -76,7 +76,7 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
     double *ev = ws + 4 * npad, *es = ws + 5 * npad;
     double *bufs = ws + (size_t)kLbfgsVecs * npad;
     const int m = cfg.m;
-    if (t == 0) {
+    if (threadIdx.x == 0) {
         sh.nslots = 0;
         for (int k = 0; k < m; ++k) {
             sh.sbuf[k] = k;
@@ -85,7 +85,7 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
         sh.stmp = m;
         sh.ytmp = 2 * m + 1;
     }
-    __syncthreads();
+    T.sync();
 
     qew_lbfgs_result res;
     res.iterations = 0;
@@ -99,12 +99,12 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
     double phi = 0.0;
     bool done = false;
 
-    block_gradient<Noise, BS>(nz, h, n, dx, lt, f, arc, ev, es, g);
+    team_gradient<Noise>(T, nz, h, n, dx, lt, f, arc, ev, es, g);
 
     for (int it = 0; it < cfg.max_iter; ++it) {
         double lm = 0.0;
-        for (int i = t; i < n; i += BS) lm = fmax(lm, fabs(g[i]));
-        const double gmax = bmax_all<BS>(lm, s_w);
+        for (int i = t0; i < n; i += ts) lm = fmax(lm, fabs(g[i]));
+        const double gmax = T.max(lm);
         if (gmax < cfg.ftol) {  // lbfgs.h:155-161
             res.iterations = it;
             res.max_force = gmax;
@@ -113,72 +113,72 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
             break;
         }
         // two-loop recursion, lbfgs.h:163-191
-        for (int i = t; i < n; i += BS) q[i] = g[i];
-        __syncthreads();
+        for (int i = t0; i < n; i += ts) q[i] = g[i];
+        T.sync();
         const int hs = sh.nslots;
         for (int idx = hs - 1; idx >= 0; --idx) {
             const int row = sh.slots[idx];
             const double *S = bufs + (size_t)sh.sbuf[row] * npad;
             const double *Y = bufs + (size_t)sh.ybuf[row] * npad;
             double acc = 0.0;
-            for (int i = t; i < n; i += BS) acc += S[i] * q[i];
-            const double a = sh.rho[row] * bsum_all<BS>(acc, s_w);
-            if (t == 0) sh.la[idx] = a;
-            for (int i = t; i < n; i += BS) q[i] += -a * Y[i];
-            __syncthreads();
+            for (int i = t0; i < n; i += ts) acc += S[i] * q[i];
+            const double a = sh.rho[row] * T.sum(acc);
+            if (threadIdx.x == 0) sh.la[idx] = a;
+            for (int i = t0; i < n; i += ts) q[i] += -a * Y[i];
+            T.sync();
         }
         if (cfg.precondition) {
-            block_precond<BS>(q, d, n, pc, s_b, s_w);
+            team_precond(T, q, d, n, pc, s_b, s_agg);
         } else {
             const double g0 = (hs == 0) ? 1.0 : gamma;
-            for (int i = t; i < n; i += BS) d[i] = g0 * q[i];
-            __syncthreads();
+            for (int i = t0; i < n; i += ts) d[i] = g0 * q[i];
+            T.sync();
         }
         for (int idx = 0; idx < hs; ++idx) {
             const int row = sh.slots[idx];
             const double *S = bufs + (size_t)sh.sbuf[row] * npad;
             const double *Y = bufs + (size_t)sh.ybuf[row] * npad;
             double acc = 0.0;
-            for (int i = t; i < n; i += BS) acc += Y[i] * d[i];
-            const double b = sh.rho[row] * bsum_all<BS>(acc, s_w);
+            for (int i = t0; i < n; i += ts) acc += Y[i] * T.ld(d + i);
+            const double b = sh.rho[row] * T.sum(acc);
             const double c = sh.la[idx] - b;
-            for (int i = t; i < n; i += BS) d[i] += c * S[i];
-            __syncthreads();
+            for (int i = t0; i < n; i += ts) d[i] = T.ld(d + i) + c * S[i];
+            T.sync();
         }
         // d = -d, fused with dphi0 = g.d (lbfgs.h:190-194)
         double acc = 0.0;
-        for (int i = t; i < n; i += BS) {
-            const double v = -d[i];
+        for (int i = t0; i < n; i += ts) {
+            const double v = -T.ld(d + i);
             d[i] = v;
             acc += g[i] * v;
         }
-        double dphi0 = bsum_all<BS>(acc, s_w);
+        double dphi0 = T.sum(acc);
         bool empty = (hs == 0);
         if (dphi0 >= 0) {  // steepest-descent fallback, lbfgs.h:195-200
-            if (t == 0) sh.nslots = 0;
+            if (threadIdx.x == 0) sh.nslots = 0;
             empty = true;
             double gg = 0.0;
-            for (int i = t; i < n; i += BS) {
+            for (int i = t0; i < n; i += ts) {
                 d[i] = -g[i];
                 gg += g[i] * g[i];
             }
-            dphi0 = -bsum_all<BS>(gg, s_w);
+            dphi0 = -T.sum(gg);
         }
         // Armijo backtracking, lbfgs.h:202-238
         if (it == 0) {
-            phi = block_objective<Noise, BS>(nz, h, d, 0.0, n, dx, lt, f, model, s_w);
+            phi = team_objective<Noise>(T, nz, h, d, 0.0, n, dx, lt, f, model);
             ++res.n_func_evals;
         }
         const double phi0 = phi;
         double alpha = 1.0;
         if (!cfg.precondition && empty) {
             double gg = 0.0;
-            for (int i = t; i < n; i += BS) gg += g[i] * g[i];
-            alpha = 1.0 / fmax(1.0, sqrt(bsum_all<BS>(gg, s_w)));
+            for (int i = t0; i < n; i += ts) gg += g[i] * g[i];
+            alpha = 1.0 / fmax(1.0, sqrt(T.sum(gg)));
         }
         bool ok = false, have_gn = false;
         for (int ls = 0; ls < cfg.max_ls; ++ls) {
-            const double pt = block_objective<Noise, BS>(nz, h, d, alpha, n, dx, lt, f, model, s_w);
+            const double pt = team_objective<Noise>(T, nz, h, d, alpha, n, dx, lt, f, model);
             ++res.n_func_evals;
             if (pt <= phi0 + cfg.c1 * alpha * dphi0) {
                 phi = pt;
@@ -186,12 +186,12 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
                 break;
             }
             if (cfg.ls_fallback) {  // slope test at the trial point, q = h + alpha d
-                for (int i = t; i < n; i += BS) q[i] = h[i] + alpha * d[i];
-                __syncthreads();
-                block_gradient<Noise, BS>(nz, q, n, dx, lt, f, arc, ev, es, gn);
+                for (int i = t0; i < n; i += ts) q[i] = h[i] + alpha * d[i];
+                T.sync();
+                team_gradient<Noise>(T, nz, q, n, dx, lt, f, arc, ev, es, gn);
                 double sd = 0.0;
-                for (int i = t; i < n; i += BS) sd += gn[i] * d[i];
-                const double dphia = bsum_all<BS>(sd, s_w);
+                for (int i = t0; i < n; i += ts) sd += gn[i] * d[i];
+                const double dphia = T.sum(sd);
                 ++res.n_func_evals;
                 if (dphia >= kAwSigma * dphi0 && dphia <= (2.0 * kAwDelta - 1.0) * dphi0 &&
                     pt <= phi0 + kAwEps * fabs(phi0)) {
@@ -211,19 +211,19 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
                 done = true;
                 break;
             }
-            if (t == 0) sh.nslots = 0;
+            if (threadIdx.x == 0) sh.nslots = 0;
             ++res.n_ls_restarts;
-            __syncthreads();
+            T.sync();
             continue;
         }
         ls_fail_streak = 0;
-        for (int i = t; i < n; i += BS) h[i] += alpha * d[i];  // lbfgs.h:243-244
-        __syncthreads();
-        if (!have_gn) block_gradient<Noise, BS>(nz, h, n, dx, lt, f, arc, ev, es, gn);
+        for (int i = t0; i < n; i += ts) h[i] += alpha * d[i];  // lbfgs.h:243-244
+        T.sync();
+        if (!have_gn) team_gradient<Noise>(T, nz, h, n, dx, lt, f, arc, ev, es, gn);
         double *sT = bufs + (size_t)sh.stmp * npad;
         double *yT = bufs + (size_t)sh.ytmp * npad;
         double sy = 0.0, ss = 0.0, yy = 0.0;
-        for (int i = t; i < n; i += BS) {  // lbfgs.h:250-261
+        for (int i = t0; i < n; i += ts) {  // lbfgs.h:250-261
             const double s = alpha * d[i];
             const double y = gn[i] - g[i];
             sT[i] = s;
@@ -232,9 +232,9 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
             ss += s * s;
             yy += y * y;
         }
-        bsum3_all<BS>(sy, ss, yy, s_w);
+        T.sum3(sy, ss, yy);
         if (sy > cfg.curvature_eps * sqrt(ss * yy)) {  // lbfgs.h:262-279
-            if (t == 0) {
+            if (threadIdx.x == 0) {
                 int row;
                 if (sh.nslots < m) {
                     row = sh.nslots;
@@ -256,19 +256,31 @@ __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h,
         } else {
             ++res.n_curvature_skips;
         }
-        __syncthreads();
+        T.sync();
         double *tg = g;
         g = gn;
         gn = tg;
     }
     if (!done) {  // lbfgs.h:283-286
         double lm = 0.0;
-        for (int i = t; i < n; i += BS) lm = fmax(lm, fabs(g[i]));
+        for (int i = t0; i < n; i += ts) lm = fmax(lm, fabs(g[i]));
         res.iterations = cfg.max_iter;
-        res.max_force = bmax_all<BS>(lm, s_w);
+        res.max_force = T.max(lm);
         res.converged = 0;
     }
     return res;  // identical in every thread
+}
+
+
+// One CTA runs the whole solve (the single-line resident form and the
+// ensemble's CTA per line).
+template <class Noise, int BS>
+__device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h, const int n,
+                                        const qew_params P, const LbfgsCfg cfg,
+                                        const PrecondCoef pc, double *ws, size_t npad) {
+    __shared__ double s_w[96];
+    CtaTeam<BS> T{s_w};
+    return lbfgs_team<Noise>(T, nz, h, n, P, cfg, pc, ws, npad);
 }
 
 size_t qew_lbfgs_resident_ws_doubles(int n, int m);

@@ -5,15 +5,17 @@
 // order, Larkin map Gamma = amplitude * (lambda_p/xi)^1.5 (qew_runs.h:27-34),
 // flat start at Ly/2 and the results are the reference's; the work inside
 // each step runs on the GPU:
-//   * static_sweep: the ratios are independent lines, relaxed together by
-//     one persistent ensemble launch on a B-spline field (FP64 throughout),
-//     else one resident L-BFGS solve after another;
+//   * static_sweep: the ratios are independent lines, relaxed together in one
+//     launch -- a thread-block cluster per line for long lines, else the
+//     ensemble kernel's CTA per line on a B-spline field (FP64 throughout) --
+//     or one resident L-BFGS solve after another;
 //   * dynamic_anneal: the per-step anneal coefficients are produced on the
 //     host exactly as the reference's loop does, and the steps between two
 //     snapshots run device-resident (qew_langevin_run);
 //   * depinning_ramp: resident rk_block per force, restarting from the last
 //     configuration; optionally a force bisection to f_c afterwards.
 #include "qew_internal.cuh"
+#include "qew_lbfgs_internal.cuh"
 #include "qew_runs.h"
 
 #include <cmath>
@@ -117,18 +119,27 @@ qew_status qew_static_sweep(qew_ctx *ctx, const qew_field *field, const qew_stat
         profiles[k].line_tension = p.line_tension;
     }
     std::vector<qew_lbfgs_result> res(K);
-    if (field->kind == QEW_FIELD_BSPLINE && field->coef64) {
-        std::vector<qew_ensemble_line> el(K);
-        for (int k = 0; k < K; ++k)
-            el[k] = qew_ensemble_line{field, lines.d + (size_t)k * n, n, ps[k], lp.precond_shift};
-        qew_ensemble_params ep{};
-        ep.lbfgs = lp;
-        ep.ftol_fp32 = 0.0;  // FP64 throughout, as the reference
-        QEW_TRY(qew_ensemble_minimize(ctx, K, el.data(), &ep, res.data()));
-    } else {
-        for (int k = 0; k < K; ++k)
-            QEW_TRY(qew_lbfgs_minimize(ctx, field, lines.d + (size_t)k * n, n, &ps[k], &lp,
-                                       &res[k]));
+    // long lines: one thread-block cluster per ratio; else the ensemble kernel
+    // (one CTA per ratio) on a B-spline field, or one solve after another
+    std::vector<double *> hp(K);
+    std::vector<double> shifts(K, lp.precond_shift);
+    for (int k = 0; k < K; ++k) hp[k] = lines.d + (size_t)k * n;
+    const qew_status cs = qew_lbfgs_cluster_lines(ctx, field, K, hp.data(), n, ps.data(),
+                                                  shifts.data(), &lp, res.data());
+    if (cs != QEW_OK && cs != QEW_ERR_UNSUPPORTED) return cs;
+    if (cs == QEW_ERR_UNSUPPORTED) {
+        if (field->kind == QEW_FIELD_BSPLINE && field->coef64) {
+            std::vector<qew_ensemble_line> el(K);
+            for (int k = 0; k < K; ++k)
+                el[k] = qew_ensemble_line{field, hp[k], n, ps[k], lp.precond_shift};
+            qew_ensemble_params ep{};
+            ep.lbfgs = lp;
+            ep.ftol_fp32 = 0.0;  // FP64 throughout, as the reference
+            QEW_TRY(qew_ensemble_minimize(ctx, K, el.data(), &ep, res.data()));
+        } else {
+            for (int k = 0; k < K; ++k)
+                QEW_TRY(qew_lbfgs_minimize(ctx, field, hp[k], n, &ps[k], &lp, &res[k]));
+        }
     }
     QEW_CUDA(ctx, cudaMemcpyAsync(h_out, lines.d, (size_t)K * n * sizeof(double),
                                   cudaMemcpyDeviceToHost, ctx->stream));

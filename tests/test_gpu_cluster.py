@@ -1,0 +1,104 @@
+"""L-BFGS of long lines on a thread-block cluster (qew_team.cuh): the same
+solve as one CTA up to reduction order, against the one-CTA form (the
+ensemble kernel), the oracle and the reference's known answers."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import band_limited_field
+
+pytestmark = pytest.mark.gpu
+
+
+def t64(a):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def npy(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [2048, 4096, 16384])
+def test_harmonic_well_known_answer(Q, n):
+    """test_lbfgs.cpp: line tension + harmonic trough relaxes to h = y0."""
+    h = t64(np.zeros(n))
+    r = Q.lbfgs_minimize(h, Q.Params(float(n), 1.0, 0.0, Q.Model.Linear), Q.HarmonicWell(2.0, 0.5),
+                         Q.LbfgsParams(ftol=1e-10, precondition=True))
+    assert r.converged
+    assert np.max(np.abs(npy(h) - 0.5)) < 1e-8
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("n", [4096, 8192])
+def test_cluster_matches_one_cta_form(Q, model, n):
+    """Same solve by a cluster (lbfgs_minimize) and by one CTA (the ensemble
+    kernel): both converge to the same minimum; energies agree to 1e-12. (On
+    this stiff line, dx = 0.1, every form -- cluster, one CTA, the oracle --
+    stalls near max|g| ~ 1e-7, so the tolerance is 1e-7.)"""
+    ny, Lx, Ly = 64, float(n) / 10, 1.0
+    f = Q.FilteredNoise(band_limited_field(n, ny, Lx, Ly, 0.4, 0.3, 5), Lx, Ly)
+    p = Q.Params(Lx, 1.5, 0.0, Q.Model(model))
+    lp = Q.LbfgsParams(m=10, ftol=1e-7, max_iter=20000, precondition=True, precond_shift=0.2,
+                       ls_fallback=True)
+    h0 = 0.5 + 0.02 * np.sin(2 * np.pi * np.arange(n) / n)
+    h1, h2 = t64(h0), t64(h0)
+    r1 = Q.lbfgs_minimize(h1, p, f, lp)
+    r2 = Q.ensemble_minimize([(h2, p, f, 0.2)], lp)[0]
+    assert r1.converged and r2.converged
+    e1, e2 = Q.objective(h1, p, f), Q.objective(h2, p, f)
+    assert abs(e1 - e2) <= 1e-12 * abs(e2)
+    assert np.max(np.abs(npy(h1) - npy(h2))) < 1e-6
+    assert abs(r1.iterations - r2.iterations) <= max(10, r2.iterations // 5)
+
+
+def test_cluster_deterministic(Q):
+    n, ny, Lx, Ly = 4096, 64, 409.6, 1.0
+    f = Q.FilteredNoise(band_limited_field(n, ny, Lx, Ly, 0.4, 0.3, 6), Lx, Ly)
+    p = Q.Params(Lx, 1.0, 0.0, Q.Model.Arclength)
+    lp = Q.LbfgsParams(ftol=1e-8, precondition=True, precond_shift=0.1)
+    h1, h2 = t64(np.full(n, 0.5)), t64(np.full(n, 0.5))
+    r1, r2 = Q.lbfgs_minimize(h1, p, f, lp), Q.lbfgs_minimize(h2, p, f, lp)
+    assert r1.iterations == r2.iterations and r1.n_func_evals == r2.n_func_evals
+    assert np.array_equal(npy(h1), npy(h2))
+
+
+def test_cluster_matches_oracle(Q, O):
+    """Against the oracle's serial lbfgs_minimize on the same field."""
+    n, ny, Lx, Ly = 2048, 48, 204.8, 1.0
+    fld = band_limited_field(n, ny, Lx, Ly, 0.3, 0.3, 9)
+    f = Q.FilteredNoise(fld, Lx, Ly)
+    of = O.BSplineField(fld, Lx, Ly)
+    h = t64(np.full(n, 0.5))
+    r = Q.lbfgs_minimize(h, Q.Params(Lx, 2.0, 0.0, Q.Model.Linear), f,
+                         Q.LbfgsParams(ftol=1e-7, precondition=True, precond_shift=0.1,
+                                       ls_fallback=True))
+    hc = np.full(n, 0.5)
+    rc = O.lbfgs_minimize(hc, O.params(Lx, 2.0, 0.0, 0), of,
+                          O.lbfgs_default_params(ftol=1e-7, precondition=1, precond_shift=0.1,
+                                                 ls_fallback=1))
+    assert r.converged and rc.converged
+    assert np.max(np.abs(npy(h) - hc)) < 1e-5
+    e = Q.objective(h, Q.Params(Lx, 2.0, 0.0, Q.Model.Linear), f)
+    ec = O.objective(hc, O.params(Lx, 2.0, 0.0, 0), of)
+    assert abs(e - ec) <= 1e-11 * abs(ec)
+
+
+def test_static_sweep_long_lines_equal_single_solves(Q):
+    """static_sweep relaxes long lines with one cluster each: line for line the
+    same as lbfgs_minimize with the driver's settings."""
+    nx, ny, Lx, Ly, xi = 4096, 64, 32.0, 1.0, 0.1
+    f = Q.FilteredNoise.seeded(nx, ny, Lx, Ly, 1.0, xi, xi, 3)
+    c = Q.StaticConfig(model=Q.Model.Arclength, xi=xi, Lx=Lx, Ly=Ly, nx=nx, ny=ny,
+                       pinning_lengths_over_xi=(1.0, 10.0), ftol=1e-6, max_iter=5000)
+    prof = Q.static_sweep(c, f)
+    for p in prof:
+        h = t64(np.full(nx, 0.5 * Ly))
+        lp = Q.LbfgsParams(ftol=c.ftol, max_iter=c.max_iter, precondition=True,
+                           precond_shift=0.5 * (Lx / nx) / xi ** 2)
+        r = Q.lbfgs_minimize(h, Q.Params(Lx, p.line_tension, 0.0, Q.Model.Arclength), f, lp)
+        assert r.iterations == p.result.iterations
+        assert np.array_equal(npy(h), p.h)
