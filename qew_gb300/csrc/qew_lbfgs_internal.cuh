@@ -13,13 +13,14 @@ qew_status qew_lbfgs_resident(qew_ctx *ctx, const qew_field *field, double *d_h,
                               const qew_params *p, const qew_lbfgs_params *lp,
                               qew_lbfgs_result *res);
 // Relaxes `count` lines of n points (d_h[k], parameters ps[k], preconditioner
-// shift shifts[k]) on one field, one thread-block cluster per line. Returns
+// shift shifts[k]) on one field, one thread-block cluster per line; precision
+// QEW_PREC_FP32_SPLIT gathers the field's FP32 coefficients. Returns
 // QEW_ERR_UNSUPPORTED (recording nothing) when the lines are too short for a
 // cluster or the device cannot run one; the caller then uses another form.
 qew_status qew_lbfgs_cluster_lines(qew_ctx *ctx, const qew_field *field, int count,
                                    double *const *d_h, int n, const qew_params *ps,
                                    const double *shifts, const qew_lbfgs_params *lp,
-                                   qew_lbfgs_result *res);
+                                   qew_lbfgs_result *res, int precision = QEW_PREC_FP64);
 qew_status qew_precond_plain(qew_ctx *ctx, const double *d_q, int n, double kappa,
                              double physical_size, double shift, double *d_out);
 qew_status qew_precond_resident(qew_ctx *ctx, const double *d_q, int n, double kappa,

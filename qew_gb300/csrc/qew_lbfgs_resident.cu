@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "qew_lbfgs_internal.cuh"
+#include "qew_noise32.cuh"
 #include "qew_lbfgs_resident.cuh"
 
 PrecondCoef qew_precond_coef(int n, double kappa, double physical_size, double shift) {
@@ -213,7 +214,7 @@ qew_status qew_lbfgs_resident(qew_ctx *ctx, const qew_field *field, double *d_h,
 qew_status qew_lbfgs_cluster_lines(qew_ctx *ctx, const qew_field *field, int count,
                                    double *const *d_h, int n, const qew_params *ps,
                                    const double *shifts, const qew_lbfgs_params *lp,
-                                   qew_lbfgs_result *res) {
+                                   qew_lbfgs_result *res, int precision) {
     if (count < 1 || lp->m > kLbfgsMaxM) return QEW_ERR_UNSUPPORTED;
     std::vector<ClusterLine> lines(count);
     for (int k = 0; k < count; ++k) {
@@ -224,12 +225,18 @@ qew_status qew_lbfgs_cluster_lines(qew_ctx *ctx, const qew_field *field, int cou
                                        : PrecondCoef{};
     }
     bool clustered = false;
-    QEW_TRY(qew_dispatch_noise(ctx, field, [&](auto nz) -> qew_status {
+    auto run = [&](auto nz) -> qew_status {
         const int csize = cluster_size_for<decltype(nz)>(ctx, n);
         if (!csize) return QEW_OK;
         clustered = true;
         return lbfgs_cluster_launch(ctx, nz, csize, lines, n, lp, res);
-    }, n, ps[0].physical_size));
+    };
+    if (precision == QEW_PREC_FP32_SPLIT) {
+        if (field->kind != QEW_FIELD_BSPLINE || !field->coef32) return QEW_ERR_UNSUPPORTED;
+        QEW_TRY(run(make_split32(field, n, ps[0].physical_size)));
+    } else {
+        QEW_TRY(qew_dispatch_noise(ctx, field, run, n, ps[0].physical_size));
+    }
     return clustered ? QEW_OK : QEW_ERR_UNSUPPORTED;
 }
 

@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "qew_internal.cuh"
+#include "qew_lbfgs_internal.cuh"
 #include "qew_rk_internal.cuh"
 #include "qew_vec.cuh"
 
@@ -82,7 +83,24 @@ qew_status run_static(qew_ctx *ctx, const qew_request &r, qew_field *f, double *
     ep.ftol_fp32 = 2e-5;
     ep.max_iter_fp32 = 0;
     qew_lbfgs_result res;
-    QEW_TRY(qew_ensemble_minimize(ctx, 1, &line, &ep, &res));
+    // a long line runs on a thread-block cluster (both phases), else on one CTA
+    double *hp[1] = {h};
+    const double shift[1] = {line.precond_shift};
+    qew_lbfgs_params lp32 = ep.lbfgs;
+    lp32.ftol = ep.ftol_fp32;
+    qew_lbfgs_result r32{};
+    qew_status cs = qew_lbfgs_cluster_lines(ctx, f, 1, hp, r.n, &line.p, shift, &lp32, &r32,
+                                            QEW_PREC_FP32_SPLIT);
+    if (cs == QEW_OK)
+        cs = qew_lbfgs_cluster_lines(ctx, f, 1, hp, r.n, &line.p, shift, &ep.lbfgs, &res);
+    if (cs == QEW_OK) {
+        res.iterations += r32.iterations;
+        res.n_func_evals += r32.n_func_evals;
+    } else if (cs == QEW_ERR_UNSUPPORTED) {
+        QEW_TRY(qew_ensemble_minimize(ctx, 1, &line, &ep, &res));
+    } else {
+        return cs;
+    }
     out.iterations = res.iterations;
     out.max_force = res.max_force;
     out.converged = res.converged;
