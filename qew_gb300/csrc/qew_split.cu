@@ -71,9 +71,11 @@ __device__ __forceinline__ void edge_x(const SplitGeom &g, int e, int &ix, float
     ix = min(max(c, 0), g.nx - 1);
 }
 
-// dV/dy at (ix + fx, cy + fy) cells on FP32 coefficients.
-__device__ __forceinline__ float split_dvdy(const float *__restrict__ coef, int nx, int ny, int ix,
-                                            float fx, int cy, float fy, float inv_dy) {
+// dV/dy at (ix + fx, cy + fy) cells on FP32 coefficients (any stencil,
+// wrapping around the field on either axis).
+__device__ __forceinline__
+float split_dvdy(const float *__restrict__ coef, int nx, int ny, int ix, float fx, int cy,
+                 float fy, float inv_dy) {
     int xs[4], ys[4];
     wrap4(ix, nx, xs);
     wrap4(wrap_cell(cy, ny), ny, ys);
