@@ -59,6 +59,9 @@ __global__ void __launch_bounds__(BS) k_precond_resident(const double *q, double
 
 constexpr int kClusterBS = 256;
 constexpr int kClusterMinN = 2048;
+#ifndef QEW_CLUSTER_POINTS_PER_THREAD
+#define QEW_CLUSTER_POINTS_PER_THREAD 1  // build-time tuning knob (measured on GB300)
+#endif
 
 // One line of a cluster launch (all lines of a launch share n and the field).
 struct ClusterLine {
@@ -95,14 +98,17 @@ k_lbfgs_single(Noise nz, double *h, int n, qew_params P, LbfgsCfg cfg, PrecondCo
 
 }  // namespace
 
-// Cluster size for a line of n points: about 2 points per thread, a power of
-// two between 4 and 16 CTAs, 0 when the line is too short or the device
-// cannot co-schedule such a cluster (the one-CTA form is used then).
+// Cluster size for a line of n points: about QEW_CLUSTER_POINTS_PER_THREAD
+// points per thread, a power of two between 4 and 16 CTAs, 0 when the line is
+// too short or the device cannot co-schedule such a cluster (the one-CTA
+// form is used then).
 template <class Noise>
 static int cluster_size_for(qew_ctx *ctx, int n) {
     if (n < kClusterMinN) return 0;
     int c = 1;
-    while (c < kTeamMaxCtas && (long long)c * 2 * kClusterBS * 2 <= n) c *= 2;
+    while (c < kTeamMaxCtas &&
+           (long long)c * 2 * kClusterBS * QEW_CLUSTER_POINTS_PER_THREAD <= n)
+        c *= 2;
     if (c < 4) return 0;
     auto kern = k_lbfgs_cluster<Noise, kClusterBS>;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
