@@ -186,3 +186,72 @@ __device__ __forceinline__ double rk_forward_zero_group(const Noise &nz, int i, 
     found = true;
     return 0.5 * (lo + hc);
 }
+
+// rk_site_velocity evaluated by a lane pair (lanes `lane` = 0 and 1 of an
+// aligned pair, same site and heights): each lane gathers one of the two edge
+// midpoints, the other one's value comes by shuffle, and both finish the
+// same expression -- the value is rk_site_velocity's bit for bit.
+template <class Noise>
+__device__ __forceinline__ double rk_site_velocity_pair(const Noise &nz, int i, int n, double dx,
+                                                        double lt, double f, int model, double hi,
+                                                        double hl, double hr, int lane,
+                                                        unsigned pmask) {
+    const int im = (i == 0) ? n - 1 : i - 1;
+    const int ip = (i + 1 == n) ? 0 : i + 1;
+    double line_force;
+    if (model == QEW_MODEL_LINEAR) {
+        line_force = -lt * (hl + hr - 2.0 * hi) / (dx * dx);
+    } else {
+        const double dhr = (hr - hi) / dx;
+        const double dhl = (hi - hl) / dx;
+        line_force = lt * (dhl / sqrt(1.0 + dhl * dhl) - dhr / sqrt(1.0 + dhr * dhr)) / dx;
+    }
+    const double xc = lane ? (double)(i + ip) * 0.5 * dx : (double)(im + i) * 0.5 * dx;
+    const double hc = lane ? (hi + hr) * 0.5 : (hl + hi) * 0.5;
+    const double mine = nz.dvdy(xc, hc);
+    const double other = __shfl_xor_sync(pmask, mine, 1);
+    const double dvl = lane ? other : mine;
+    const double dvr = lane ? mine : other;
+    const double grad = dx * (line_force + 0.5 * (dvl + dvr) - f);
+    return -grad;
+}
+
+// rk_forward_zero with every velocity evaluated by a lane pair
+// (rk_site_velocity_pair): the serial march and bisection, run identically by
+// both lanes, with each evaluation's two gathers side by side. Same result as
+// rk_forward_zero.
+template <class Noise>
+__device__ __forceinline__ double rk_forward_zero_pair(const Noise &nz, int i, int n, double dx,
+                                                       double lt, double f, int model, double hi,
+                                                       double hl, double hr, const RkP &rp,
+                                                       bool &found, int lane, unsigned pmask) {
+    const double v0 = rk_site_velocity_pair(nz, i, n, dx, lt, f, model, hi, hl, hr, lane, pmask);
+    if (v0 <= 0) {
+        found = true;
+        return hi;
+    }
+    double a = hi;
+    double advanced = 0;
+    while (advanced < rp.max_advance) {
+        const double b = a + rp.dstep;
+        const double vb = rk_site_velocity_pair(nz, i, n, dx, lt, f, model, b, hl, hr, lane, pmask);
+        if (vb <= 0) {
+            double lo = a, hc = b;
+            for (int k = 0; k < 60 && (hc - lo) > rp.root_tol; ++k) {
+                const double mid = 0.5 * (lo + hc);
+                const double vm =
+                    rk_site_velocity_pair(nz, i, n, dx, lt, f, model, mid, hl, hr, lane, pmask);
+                if (vm > 0)
+                    lo = mid;
+                else
+                    hc = mid;
+            }
+            found = true;
+            return 0.5 * (lo + hc);
+        }
+        a = b;
+        advanced += rp.dstep;
+    }
+    found = false;
+    return a;
+}

@@ -28,8 +28,9 @@ constexpr int kRkBS = 32;  // one warp per CTA: a 16384-site line still spreads 
 #define QEW_RK_WARPS_PER_SM 4  // build-time tuning knob (measured on GB300)
 #endif
 // kRkGroup lanes per site (8: 7 march points or 3 bisection levels per round;
-// 4: 3 points or 2 levels; 1: the serial search). All sizes give the same
-// result; the launch picks one by the budget below.
+// 4: 3 points or 2 levels; 2: the serial search with each velocity's two
+// gathers on the two lanes; 1: the serial search). All widths give the same
+// result; the launch picks one by the budgets below.
 template <class Noise, int kRkGroup>
 __global__ void __launch_bounds__(kRkBS)
 k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n, double dx,
@@ -69,6 +70,10 @@ k_rk_resident(Noise nz, double *__restrict__ h, double *__restrict__ adv, int n,
                 if constexpr (kRkGroup == 1) {
                     hnew = rk_forward_zero(nz, i, n, dx, lt, f, model, hi, __ldcg(h + im),
                                            __ldcg(h + ip), rp, found);
+                } else if constexpr (kRkGroup == 2) {
+                    hnew = rk_forward_zero_pair(nz, i, n, dx, lt, f, model, hi, __ldcg(h + im),
+                                                __ldcg(h + ip), rp, found, glane, gmask);
+                    __syncwarp(gmask);  // both lanes have read h[i]
                 } else {
                     hnew = rk_forward_zero_group<kRkGroup>(nz, i, n, dx, lt, f, model, hi,
                                                           __ldcg(h + im), __ldcg(h + ip), rp,
@@ -119,16 +124,19 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
     const RkP rk = rkp_from(rp);
     auto launch = [&](auto nz) -> qew_status {
         using N = decltype(nz);
-        // the widest group whose grid stays within QEW_RK_WARPS_PER_SM warps per
-        // SM (and the resident slots, or the context's share of them): wider
-        // groups shorten each site's chain of dependent evaluations but
-        // multiply its FP64 work, which pays only while the SMs' FP64 pipes
-        // idle; the serial form takes what is left
-        // (a 2-lane group would evaluate one bisection level per round, like
-        // the serial search, at twice the work: never worth it)
-        const void *forms[3] = {(const void *)k_rk_resident<N, 8>, (const void *)k_rk_resident<N, 4>,
+        // The search width: wider groups shorten each site's chain of
+        // dependent evaluations but multiply its FP64 work, which pays only
+        // while the SMs' FP64 pipes idle; lane pairs split each evaluation's
+        // two gathers (the same FP64 work in half the chain). Each form has a
+        // warps-per-SM budget (and the resident slots, or the context's share
+        // of them); the serial form takes what is left.
+        // Measured (sweeps/s, bitwise-equal results): 8-lane groups win while
+        // they stay within about 2 warps per SM, lane pairs up to about 4,
+        // the serial search beyond; 4-lane groups were never the best.
+        const void *forms[3] = {(const void *)k_rk_resident<N, 8>, (const void *)k_rk_resident<N, 2>,
                                 (const void *)k_rk_resident<N, 1>};
-        const int sizes[3] = {8, 4, 1};
+        const int sizes[3] = {8, 2, 1};
+        const long long warps_per_sm[3] = {QEW_RK_WARPS_PER_SM / 2, QEW_RK_WARPS_PER_SM, 0};
         const long long half = n / 2;
         const void *kern = nullptr;
         int grid = 1;
@@ -137,8 +145,7 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
             QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forms[k], kRkBS, 0));
             int slots = ctx->num_sms * std::max(per_sm, 1);
             if (ctx->warp_cap > 0) slots = std::min(slots, ctx->warp_cap / (kRkBS / 32));
-            const long long budget =
-                std::min<long long>(slots, (long long)QEW_RK_WARPS_PER_SM * ctx->num_sms);
+            const long long budget = std::min<long long>(slots, warps_per_sm[k] * ctx->num_sms);
             const long long want = (half * sizes[k] + kRkBS - 1) / kRkBS;
             if (want <= budget || k == 2) {
                 kern = forms[k];

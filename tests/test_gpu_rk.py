@@ -5,7 +5,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import band_limited_field
+from conftest import band_limited_field, gaussian_field
 
 pytestmark = pytest.mark.gpu
 PI = 3.14159265358979323846
@@ -180,3 +180,22 @@ def test_bisect_fp32_close_to_fp64(Q):
     fb = Q.depinning_bisect(hb, p, f, rp, 0.0, 4.0, rtol=1e-6, max_steps=60,
                             precision=Q.QEW_PREC_FP32_SPLIT)[0]
     assert abs(fa - fb) < 1e-4 * fa
+
+
+@pytest.mark.parametrize("n", [4096, 16384, 32768])
+def test_resident_equals_plain_bitwise_long_lines(Q, n):
+    """Long lines take the other search widths of the resident kernel (8-lane
+    groups, lane-pair evaluations, one thread per site): still the plain
+    form's lines and verdicts, bit for bit."""
+    ny = 64
+    f = Q.FilteredNoise(gaussian_field(n, ny, 3.0, n % 97), float(n), float(ny))
+    rp = rkp(Q, 0.5, float(ny), 1e-10, 1e-8, 2.0 * ny, 60)
+    rng = np.random.default_rng(n)
+    h0 = ny / 2 + np.cumsum(rng.standard_normal(n)) * 0.05
+    for fdr in (0.05, 0.3):
+        p = Q.Params(float(n), 1.0, fdr, Q.Model.Linear)
+        h1, h2 = t64(h0), t64(h0)
+        r1 = Q.rk_block(h1, p, f, rp, form=Q.QEW_RK_PLAIN)
+        r2 = Q.rk_block(h2, p, f, rp, form=Q.QEW_RK_RESIDENT)
+        assert (r1.blocked, r1.runaway, r1.sweeps) == (r2.blocked, r2.runaway, r2.sweeps)
+        assert np.array_equal(npy(h1), npy(h2))
