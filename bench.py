@@ -91,6 +91,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(torch, t_ms: float, device) -> float:
+    """The slowest replica's time: the whole job ends when it does."""
+    t = torch.tensor([t_ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(ws: int, steps: int, lines: int, L: int, t_ms: float) -> float:
+    """Points per second of all replicas together (each does the same work)."""
+    return ws * steps * lines * L / (t_ms * 1e-3)
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -661,14 +673,12 @@ def run_ours(args):
         torch.distributed.barrier()
     t_ms, launches = timed(torch, step_main, args.steps, ctx)
     if ws > 1:
-        t = torch.tensor([t_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(t.item())
+        t_ms = max_over_ranks(torch, t_ms, "cuda")
         torch.distributed.barrier()
     clk = clocks.stop() if not args.profile_run else None
     t2_ms, launches2 = timed(torch, step_other, args.steps, ctx)
-    value = ws * args.steps * n_inst * L / (t_ms * 1e-3)
-    value_other = ws * args.steps * n_inst * L / (t2_ms * 1e-3)
+    value = whole_job_rate(ws, args.steps, n_inst, L, t_ms)
+    value_other = whole_job_rate(ws, args.steps, n_inst, L, t2_ms)
 
     peak, peak_kind = measured_peak()
 

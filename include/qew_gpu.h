@@ -37,7 +37,7 @@ typedef enum {
     QEW_ERR_CUDA = 3,        /* a CUDA runtime call failed */
     QEW_ERR_NOMEM = 4,       /* device allocation failed */
     QEW_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
-    QEW_ERR_UNSUPPORTED = 6  /* valid request this build does not handle */
+    QEW_ERR_UNSUPPORTED = 6  /* valid request that this library does not handle */
 } qew_status;
 
 typedef struct qew_ctx qew_ctx;

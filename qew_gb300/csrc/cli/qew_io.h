@@ -240,7 +240,7 @@ inline std::unique_ptr<Sink> open_sink(const std::string &fname) {
 #ifdef QEW_WITH_HDF5
     return std::unique_ptr<Sink>(new Hdf5Sink(fname));
 #else
-    throw std::runtime_error("this build has no HDF5 writer: give --output a .npz name (got '" +
+    throw std::runtime_error("compiled without the HDF5 writer: give --output a .npz name (got '" +
                              fname + "')");
 #endif
 }
