@@ -271,10 +271,8 @@ SplitGeom qew_split_geom(const qew_field *f, int n, const qew_params *p) {
 }
 
 // Split heights in, FP32 gradient out, `count` lines n apart.
-static qew_status split_launch(qew_ctx *ctx, const qew_field *f, const SplitGeom &g, int count,
-                               const int32_t *d_cell, const float *d_frac, float *d_grad,
-                               const char *what) {
-    (void)f;
+static qew_status split_launch(qew_ctx *ctx, const SplitGeom &g, int count, const int32_t *d_cell,
+                               const float *d_frac, float *d_grad, const char *what) {
     k_gradient_split<false, false><<<dim3((g.n + kTile - 1) / kTile, count), kBS, 0, ctx->stream>>>(
         nullptr, d_cell, d_frac, g, nullptr, d_grad);
     return qew_launch_check(ctx, what);
@@ -322,8 +320,7 @@ qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *f, const int32_t *d
     QEW_TRY(split_check(ctx, f, n, p));
     if (!d_cell || !d_frac || !d_grad)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split: null buffer");
-    return split_launch(ctx, f, qew_split_geom(f, n, p), 1, d_cell, d_frac, d_grad,
-                        "gradient_split");
+    return split_launch(ctx, qew_split_geom(f, n, p), 1, d_cell, d_frac, d_grad, "gradient_split");
 }
 
 qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *f, int count,
@@ -332,7 +329,7 @@ qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *f, int count,
     QEW_TRY(split_check(ctx, f, n, p));
     if (!d_cell || !d_frac || !d_grad || count < 1 || count > 65535)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split_batch: bad arguments");
-    return split_launch(ctx, f, qew_split_geom(f, n, p), count, d_cell, d_frac, d_grad,
+    return split_launch(ctx, qew_split_geom(f, n, p), count, d_cell, d_frac, d_grad,
                         "gradient_split_batch");
 }
 
