@@ -71,7 +71,7 @@ __global__ void k_philox_fill(double *out, int n, uint64_t seed, uint64_t step) 
 // step k uses drift[k], diff[k] and Philox step index rstep[k]. Heights are
 // double-buffered (every gradient reads the previous step's line, as the
 // reference's gradient-then-update does), one bounded grid barrier per step.
-constexpr int kRunBS = 128;
+constexpr int kRunBS = 128;  // 64 measured the same, 32 slower (L = 65536)
 constexpr int kRunTile = 2 * kRunBS;  // a thread owns one site pair (one Philox block)
 
 // Box-Muller in FP32 from the same Philox block: 24-bit uniforms, FP32
