@@ -222,6 +222,9 @@ qew_status qew_lbfgs_cluster_lines(qew_ctx *ctx, const qew_field *field, int cou
                                    const double *shifts, const qew_lbfgs_params *lp,
                                    qew_lbfgs_result *res, int precision) {
     if (count < 1 || lp->m > kLbfgsMaxM) return QEW_ERR_UNSUPPORTED;
+    // one noise functor serves every line: they must share the x geometry
+    for (int k = 1; k < count; ++k)
+        if (ps[k].physical_size != ps[0].physical_size) return QEW_ERR_UNSUPPORTED;
     std::vector<ClusterLine> lines(count);
     for (int k = 0; k < count; ++k) {
         lines[k].h = d_h[k];
