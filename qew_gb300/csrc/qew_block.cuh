@@ -104,8 +104,8 @@ __device__ double block_objective(const Noise &nz, const double *__restrict__ x0
 // the periodic closure y_{-1} = Y_end / (1 - z^n), then a second chunk pass
 // from the exact start values. In-place (out == in) is allowed. s_b needs BS
 // doubles, s_w 2*(BS/32). Ends with a barrier.
-template <int BS>
-__device__ void block_periodic_recurrence(const double *in, double *out, int n, bool rev,
+template <int BS, class R = double>
+__device__ void block_periodic_recurrence(const R *in, R *out, int n, bool rev,
                                           const PrecondCoef &pc, double *s_b, double *s_w) {
     const int t = threadIdx.x;
     const int c = (n + BS - 1) / BS;
@@ -113,7 +113,7 @@ __device__ void block_periodic_recurrence(const double *in, double *out, int n, 
     const int end = min(start + c, n);
     const double z = pc.z;
     double B = 0.0;
-    for (int k = start; k < end; ++k) B = in[rev ? n - 1 - k : k] + z * B;
+    for (int k = start; k < end; ++k) B = (double)in[rev ? n - 1 - k : k] + z * B;
     double A = (end > start) ? exp((double)(end - start) * pc.logz) : 1.0;
     // inclusive warp scan of (A, B), later element applied last
     const int lane = t & 31, w = t >> 5;
@@ -161,23 +161,24 @@ __device__ void block_periodic_recurrence(const double *in, double *out, int n, 
     double y = E;
     for (int k = start; k < end; ++k) {
         const int idx = rev ? n - 1 - k : k;
-        y = in[idx] + z * y;
-        out[idx] = y;
+        y = (double)in[idx] + z * y;
+        out[idx] = (R)y;
     }
     __syncthreads();
 }
 
-// d = M^{-1} q (lbfgs.h:173-180) as the factorised periodic solve.
-template <int BS>
-__device__ void block_precond(const double *q, double *d, int n, const PrecondCoef &pc,
-                              double *s_b, double *s_w) {
+// d = M^{-1} q (lbfgs.h:173-180) as the factorised periodic solve (vectors of
+// R, arithmetic in FP64).
+template <int BS, class R = double>
+__device__ void block_precond(const R *q, R *d, int n, const PrecondCoef &pc, double *s_b,
+                              double *s_w) {
     if (pc.scalar) {
-        for (int i = threadIdx.x; i < n; i += BS) d[i] = q[i] * pc.inv_sigma;
+        for (int i = threadIdx.x; i < n; i += BS) d[i] = (R)((double)q[i] * pc.inv_sigma);
         __syncthreads();
         return;
     }
-    block_periodic_recurrence<BS>(q, d, n, false, pc, s_b, s_w);
-    block_periodic_recurrence<BS>(d, d, n, true, pc, s_b, s_w);
-    for (int i = threadIdx.x; i < n; i += BS) d[i] *= pc.gain;
+    block_periodic_recurrence<BS, R>(q, d, n, false, pc, s_b, s_w);
+    block_periodic_recurrence<BS, R>(d, d, n, true, pc, s_b, s_w);
+    for (int i = threadIdx.x; i < n; i += BS) d[i] = (R)((double)d[i] * pc.gain);
     __syncthreads();
 }

@@ -88,7 +88,7 @@ k_ensemble(const EnsJob *__restrict__ jobs, const int *__restrict__ order, int c
         const size_t npad = ((size_t)j.n + 31) & ~size_t(31);
         (void)npad_max;
         qew_lbfgs_result r32{};
-        if (use32) r32 = lbfgs_block<NoiseSplit32, kEnsBS>(job_noise32(j), j.h, j.n, j.p, cfg32, j.pc, ws, npad);
+        if (use32) r32 = lbfgs_block<NoiseSplit32, kEnsBS, float>(job_noise32(j), j.h, j.n, j.p, cfg32, j.pc, ws, npad);
         qew_lbfgs_result r = lbfgs_block<NoiseBSpline64, kEnsBS>(job_noise64(j), j.h, j.n, j.p, cfg64, j.pc, ws, npad);
         if (threadIdx.x == 0) {
             r.iterations += r32.iterations;

@@ -6,7 +6,7 @@
 #include "qew_team.cuh"
 
 constexpr int kLbfgsMaxM = 32;
-constexpr int kLbfgsVecs = 6;  // g, g_new, d, q, edge dV/dy, edge slope
+constexpr int kLbfgsVecs = 7;  // g, g_new, d, q, edge dV/dy, edge slope, trial position
 
 struct LbfgsCfg {
     int m;
@@ -58,9 +58,12 @@ struct LbfgsShared {
     int ytmp;
 };
 
-// Workspace (npad-strided vectors): g, g_new, d, q, ev, es, then 2(m+1)
-// history buffers (m S rows + spare, m Y rows + spare).
-template <class Noise, class Team>
+// Workspace (npad doubles per vector): g, g_new, d, q, ev, es (vectors of
+// Real), the trial position xt (FP64), then 2(m+1) history buffers (m S rows
+// + spare, m Y rows + spare; Real). Real = float keeps the vectors and their
+// dot products in FP32 (a first phase on FP32 coefficients); positions,
+// energies, reductions across threads and every scalar stay FP64.
+template <class Noise, class Team, class Real = double>
 __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restrict__ h,
                                        const int n, const qew_params P, const LbfgsCfg cfg,
                                        const PrecondCoef pc, double *ws, size_t npad) {
@@ -72,9 +75,11 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
     const double lt = P.line_tension, f = P.driving_force;
     const int model = P.model;
     const bool arc = (model == QEW_MODEL_ARCLENGTH);
-    double *g = ws, *gn = ws + npad, *d = ws + 2 * npad, *q = ws + 3 * npad;
-    double *ev = ws + 4 * npad, *es = ws + 5 * npad;
+    Real *g = (Real *)ws, *gn = (Real *)(ws + npad), *d = (Real *)(ws + 2 * npad);
+    Real *q = (Real *)(ws + 3 * npad), *ev = (Real *)(ws + 4 * npad), *es = (Real *)(ws + 5 * npad);
+    double *xt = ws + 6 * npad;
     double *bufs = ws + (size_t)kLbfgsVecs * npad;
+    auto row = [&](int b) { return (Real *)(bufs + (size_t)b * npad); };
     const int m = cfg.m;
     if (threadIdx.x == 0) {
         sh.nslots = 0;
@@ -103,7 +108,7 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
 
     for (int it = 0; it < cfg.max_iter; ++it) {
         double lm = 0.0;
-        for (int i = t0; i < n; i += ts) lm = fmax(lm, fabs(g[i]));
+        for (int i = t0; i < n; i += ts) lm = fmax(lm, fabs((double)g[i]));
         const double gmax = T.max(lm);
         if (gmax < cfg.ftol) {  // lbfgs.h:155-161
             res.iterations = it;
@@ -117,52 +122,53 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
         T.sync();
         const int hs = sh.nslots;
         for (int idx = hs - 1; idx >= 0; --idx) {
-            const int row = sh.slots[idx];
-            const double *S = bufs + (size_t)sh.sbuf[row] * npad;
-            const double *Y = bufs + (size_t)sh.ybuf[row] * npad;
-            double acc = 0.0;
+            const int r = sh.slots[idx];
+            const Real *S = row(sh.sbuf[r]);
+            const Real *Y = row(sh.ybuf[r]);
+            Real acc = 0;
             for (int i = t0; i < n; i += ts) acc += S[i] * q[i];
-            const double a = sh.rho[row] * T.sum(acc);
+            const double a = sh.rho[r] * T.sum((double)acc);
             if (threadIdx.x == 0) sh.la[idx] = a;
-            for (int i = t0; i < n; i += ts) q[i] += -a * Y[i];
+            const Real na = (Real)(-a);
+            for (int i = t0; i < n; i += ts) q[i] += na * Y[i];
             T.sync();
         }
         if (cfg.precondition) {
             team_precond(T, q, d, n, pc, s_b, s_agg);
         } else {
             const double g0 = (hs == 0) ? 1.0 : gamma;
-            for (int i = t0; i < n; i += ts) d[i] = g0 * q[i];
+            for (int i = t0; i < n; i += ts) d[i] = (Real)(g0 * q[i]);
             T.sync();
         }
         for (int idx = 0; idx < hs; ++idx) {
-            const int row = sh.slots[idx];
-            const double *S = bufs + (size_t)sh.sbuf[row] * npad;
-            const double *Y = bufs + (size_t)sh.ybuf[row] * npad;
-            double acc = 0.0;
+            const int r = sh.slots[idx];
+            const Real *S = row(sh.sbuf[r]);
+            const Real *Y = row(sh.ybuf[r]);
+            Real acc = 0;
             for (int i = t0; i < n; i += ts) acc += Y[i] * T.ld(d + i);
-            const double b = sh.rho[row] * T.sum(acc);
-            const double c = sh.la[idx] - b;
+            const double b = sh.rho[r] * T.sum((double)acc);
+            const Real c = (Real)(sh.la[idx] - b);
             for (int i = t0; i < n; i += ts) d[i] = T.ld(d + i) + c * S[i];
             T.sync();
         }
         // d = -d, fused with dphi0 = g.d (lbfgs.h:190-194)
-        double acc = 0.0;
+        Real acc = 0;
         for (int i = t0; i < n; i += ts) {
-            const double v = -T.ld(d + i);
+            const Real v = -T.ld(d + i);
             d[i] = v;
             acc += g[i] * v;
         }
-        double dphi0 = T.sum(acc);
+        double dphi0 = T.sum((double)acc);
         bool empty = (hs == 0);
         if (dphi0 >= 0) {  // steepest-descent fallback, lbfgs.h:195-200
             if (threadIdx.x == 0) sh.nslots = 0;
             empty = true;
-            double gg = 0.0;
+            Real gg = 0;
             for (int i = t0; i < n; i += ts) {
                 d[i] = -g[i];
                 gg += g[i] * g[i];
             }
-            dphi0 = -T.sum(gg);
+            dphi0 = -T.sum((double)gg);
         }
         // Armijo backtracking, lbfgs.h:202-238
         if (it == 0) {
@@ -172,9 +178,9 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
         const double phi0 = phi;
         double alpha = 1.0;
         if (!cfg.precondition && empty) {
-            double gg = 0.0;
+            Real gg = 0;
             for (int i = t0; i < n; i += ts) gg += g[i] * g[i];
-            alpha = 1.0 / fmax(1.0, sqrt(T.sum(gg)));
+            alpha = 1.0 / fmax(1.0, sqrt(T.sum((double)gg)));
         }
         bool ok = false, have_gn = false;
         for (int ls = 0; ls < cfg.max_ls; ++ls) {
@@ -185,13 +191,13 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
                 ok = true;
                 break;
             }
-            if (cfg.ls_fallback) {  // slope test at the trial point, q = h + alpha d
-                for (int i = t0; i < n; i += ts) q[i] = h[i] + alpha * d[i];
+            if (cfg.ls_fallback) {  // slope test at the trial point xt = h + alpha d
+                for (int i = t0; i < n; i += ts) xt[i] = h[i] + alpha * (double)d[i];
                 T.sync();
-                team_gradient<Noise>(T, nz, q, n, dx, lt, f, arc, ev, es, gn);
-                double sd = 0.0;
+                team_gradient<Noise>(T, nz, xt, n, dx, lt, f, arc, ev, es, gn);
+                Real sd = 0;
                 for (int i = t0; i < n; i += ts) sd += gn[i] * d[i];
-                const double dphia = T.sum(sd);
+                const double dphia = T.sum((double)sd);
                 ++res.n_func_evals;
                 if (dphia >= kAwSigma * dphi0 && dphia <= (2.0 * kAwDelta - 1.0) * dphi0 &&
                     pt <= phi0 + kAwEps * fabs(phi0)) {
@@ -217,21 +223,22 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
             continue;
         }
         ls_fail_streak = 0;
-        for (int i = t0; i < n; i += ts) h[i] += alpha * d[i];  // lbfgs.h:243-244
+        for (int i = t0; i < n; i += ts) h[i] += alpha * (double)d[i];  // lbfgs.h:243-244
         T.sync();
         if (!have_gn) team_gradient<Noise>(T, nz, h, n, dx, lt, f, arc, ev, es, gn);
-        double *sT = bufs + (size_t)sh.stmp * npad;
-        double *yT = bufs + (size_t)sh.ytmp * npad;
-        double sy = 0.0, ss = 0.0, yy = 0.0;
+        Real *sT = row(sh.stmp);
+        Real *yT = row(sh.ytmp);
+        Real syr = 0, ssr = 0, yyr = 0;
         for (int i = t0; i < n; i += ts) {  // lbfgs.h:250-261
-            const double s = alpha * d[i];
-            const double y = gn[i] - g[i];
+            const Real s = (Real)(alpha * d[i]);
+            const Real y = gn[i] - g[i];
             sT[i] = s;
             yT[i] = y;
-            sy += s * y;
-            ss += s * s;
-            yy += y * y;
+            syr += s * y;
+            ssr += s * s;
+            yyr += y * y;
         }
+        double sy = syr, ss = ssr, yy = yyr;
         T.sum3(sy, ss, yy);
         if (sy > cfg.curvature_eps * sqrt(ss * yy)) {  // lbfgs.h:262-279
             if (threadIdx.x == 0) {
@@ -257,13 +264,13 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
             ++res.n_curvature_skips;
         }
         T.sync();
-        double *tg = g;
+        Real *tg = g;
         g = gn;
         gn = tg;
     }
     if (!done) {  // lbfgs.h:283-286
         double lm = 0.0;
-        for (int i = t0; i < n; i += ts) lm = fmax(lm, fabs(g[i]));
+        for (int i = t0; i < n; i += ts) lm = fmax(lm, fabs((double)g[i]));
         res.iterations = cfg.max_iter;
         res.max_force = T.max(lm);
         res.converged = 0;
@@ -274,13 +281,13 @@ __device__ qew_lbfgs_result lbfgs_team(Team &T, const Noise &nz, double *__restr
 
 // One CTA runs the whole solve (the single-line resident form and the
 // ensemble's CTA per line).
-template <class Noise, int BS>
+template <class Noise, int BS, class Real = double>
 __device__ qew_lbfgs_result lbfgs_block(const Noise &nz, double *__restrict__ h, const int n,
                                         const qew_params P, const LbfgsCfg cfg,
                                         const PrecondCoef pc, double *ws, size_t npad) {
     __shared__ double s_w[96];
     CtaTeam<BS> T{s_w};
-    return lbfgs_team<Noise>(T, nz, h, n, P, cfg, pc, ws, npad);
+    return lbfgs_team<Noise, CtaTeam<BS>, Real>(T, nz, h, n, P, cfg, pc, ws, npad);
 }
 
 size_t qew_lbfgs_resident_ws_doubles(int n, int m);

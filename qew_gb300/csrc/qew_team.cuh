@@ -39,6 +39,7 @@ struct CtaTeam {
     }
     __device__ __forceinline__ void sync() const { __syncthreads(); }
     __device__ __forceinline__ double ld(const double *p) const { return *p; }
+    __device__ __forceinline__ float ld(const float *p) const { return *p; }
 };
 
 template <int BS>
@@ -55,6 +56,7 @@ struct ClusterTeam {
     __device__ __forceinline__ unsigned size() const { return sz; }
     __device__ __forceinline__ void sync() const { cooperative_groups::this_cluster().sync(); }
     __device__ __forceinline__ double ld(const double *p) const { return __ldcg(p); }
+    __device__ __forceinline__ float ld(const float *p) const { return __ldcg(p); }
     // publish k CTA values into every CTA's slots, barrier; returns the local slots
     __device__ __forceinline__ double *publish(const double *v, int k) {
         double *buf = s_red + phase * 3 * kTeamMaxCtas;
@@ -95,37 +97,38 @@ struct ClusterTeam {
 
 // gradient() of a whole line by a team (qew_model.h:149-193): edge pass into
 // ev/es, barrier, site combine into g, barrier.
-template <class Noise, class Team>
+template <class Noise, class Team, class R>
 __device__ void team_gradient(Team &T, const Noise &nz, const double *__restrict__ h, int n,
-                              const LineDx &dx, double lt, double f, bool arc, double *ev,
-                              double *es, double *g) {
+                              const LineDx &dx, double lt, double f, bool arc, R *ev, R *es,
+                              R *g) {
     for (int e = T.tid(); e < n; e += T.stride()) {
         const int ep = (e + 1 == n) ? 0 : e + 1;
         double dv, sl;
         edge_gradient(nz, e, n, T.ld(h + e), T.ld(h + ep), dx, arc, dv, sl);
-        ev[e] = dv;
-        es[e] = sl;
+        ev[e] = (R)dv;
+        es[e] = (R)sl;
     }
     T.sync();
     for (int i = T.tid(); i < n; i += T.stride()) {
         const int ip = (i + 1 == n) ? 0 : i + 1;
         const int im = (i == 0) ? n - 1 : i - 1;
-        g[i] = site_gradient(T.ld(h + im), T.ld(h + i), T.ld(h + ip), T.ld(ev + im), T.ld(ev + i),
-                             T.ld(es + im), T.ld(es + i), dx, lt, f, arc);
+        g[i] = (R)site_gradient(T.ld(h + im), T.ld(h + i), T.ld(h + ip), (double)T.ld(ev + im),
+                                (double)T.ld(ev + i), (double)T.ld(es + im), (double)T.ld(es + i),
+                                dx, lt, f, arc);
     }
     T.sync();
 }
 
 // objective() at x0 + alpha*d by a team.
-template <class Noise, class Team>
+template <class Noise, class Team, class R>
 __device__ double team_objective(Team &T, const Noise &nz, const double *__restrict__ x0,
-                                 const double *__restrict__ d, double alpha, int n,
+                                 const R *__restrict__ d, double alpha, int n,
                                  const LineDx &dx, double lt, double f, int model) {
     double acc = 0.0;
     for (int i = T.tid(); i < n; i += T.stride()) {
         const int ip = (i + 1 == n) ? 0 : i + 1;
-        const double hi = T.ld(x0 + i) + alpha * T.ld(d + i);
-        const double hip = T.ld(x0 + ip) + alpha * T.ld(d + ip);
+        const double hi = T.ld(x0 + i) + alpha * (double)T.ld(d + i);
+        const double hip = T.ld(x0 + ip) + alpha * (double)T.ld(d + ip);
         acc += edge_energy(nz, i, ip, hi, hip, dx, lt, f, model);
     }
     return T.sum(acc);
@@ -136,9 +139,9 @@ __device__ double team_objective(Team &T, const Noise &nz, const double *__restr
 // maps is followed by a scan over the CTAs' aggregate maps (published through
 // distributed shared memory), then the periodic closure and the second chunk
 // pass. s_b: BS doubles, s_agg: 2 x kTeamMaxCtas doubles. Ends with a barrier.
-template <int BS>
-__device__ void cluster_periodic_recurrence(ClusterTeam<BS> &T, const double *in, double *out,
-                                            int n, bool rev, const PrecondCoef &pc, double *s_b,
+template <int BS, class R>
+__device__ void cluster_periodic_recurrence(ClusterTeam<BS> &T, const R *in, R *out, int n,
+                                            bool rev, const PrecondCoef &pc, double *s_b,
                                             double *s_agg) {
     const int t = threadIdx.x;
     const int G = BS * (int)T.size();
@@ -149,7 +152,7 @@ __device__ void cluster_periodic_recurrence(ClusterTeam<BS> &T, const double *in
     const int cta_start = min((int)T.rank() * BS * c, n);
     const double z = pc.z;
     double B = 0.0;
-    for (int k = start; k < end; ++k) B = __ldcg(in + (rev ? n - 1 - k : k)) + z * B;
+    for (int k = start; k < end; ++k) B = (double)__ldcg(in + (rev ? n - 1 - k : k)) + z * B;
     double A = (end > start) ? exp((double)(end - start) * pc.logz) : 1.0;
     double *s_w = T.s_w;
     const int lane = t & 31, w = t >> 5;
@@ -209,28 +212,29 @@ __device__ void cluster_periodic_recurrence(ClusterTeam<BS> &T, const double *in
     double y = cin + exp((double)start * pc.logz) * P;
     for (int k = start; k < end; ++k) {
         const int idx = rev ? n - 1 - k : k;
-        y = __ldcg(in + idx) + z * y;
-        out[idx] = y;
+        y = (double)__ldcg(in + idx) + z * y;
+        out[idx] = (R)y;
     }
     T.sync();
 }
 
 // d = M^{-1} q (lbfgs.h:173-180) by a team.
-template <class Team>
-__device__ void team_precond(Team &T, const double *q, double *d, int n, const PrecondCoef &pc,
-                             double *s_b, double *s_agg) {
+template <class Team, class R>
+__device__ void team_precond(Team &T, const R *q, R *d, int n, const PrecondCoef &pc, double *s_b,
+                             double *s_agg) {
     if constexpr (!Team::kCluster) {
         (void)s_agg;
-        block_precond<Team::kBS>(q, d, n, pc, s_b, T.s_w);
+        block_precond<Team::kBS, R>(q, d, n, pc, s_b, T.s_w);
     } else {
         if (pc.scalar) {
-            for (int i = T.tid(); i < n; i += T.stride()) d[i] = __ldcg(q + i) * pc.inv_sigma;
+            for (int i = T.tid(); i < n; i += T.stride())
+                d[i] = (R)((double)__ldcg(q + i) * pc.inv_sigma);
             T.sync();
             return;
         }
         cluster_periodic_recurrence(T, q, d, n, false, pc, s_b, s_agg);
-        cluster_periodic_recurrence(T, d, d, n, true, pc, s_b, s_agg);
-        for (int i = T.tid(); i < n; i += T.stride()) d[i] = __ldcg(d + i) * pc.gain;
+        cluster_periodic_recurrence(T, (const R *)d, d, n, true, pc, s_b, s_agg);
+        for (int i = T.tid(); i < n; i += T.stride()) d[i] = (R)((double)__ldcg(d + i) * pc.gain);
         T.sync();
     }
 }
