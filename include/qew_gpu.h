@@ -72,8 +72,15 @@ enum {
     QEW_FIELD_SINCOS = 5
 };
 
-/* Storage flags for B-spline fields. */
-enum { QEW_STORE_FP64 = 1, QEW_STORE_FP32 = 2 };
+/* Storage flags for B-spline fields. FP32_EDGE (only together with FP32)
+ * adds the coefficients filtered along x at the half-integer columns,
+ * E[j][e] = sum_a w_a(1/2) c[j][(e - 1 + a) mod nx] (computed in FP64,
+ * stored FP32): the x half of the tensor-product sum at the edge midpoints
+ * of a line with one point per field column (the x weights there are the
+ * constants w(1/2) = 1/48, 23/48, 23/48, 1/48). With it the split-form
+ * gradient on such a line reads 4 values per edge instead of 16; every other
+ * line and call ignores it. */
+enum { QEW_STORE_FP64 = 1, QEW_STORE_FP32 = 2, QEW_STORE_FP32_EDGE = 4 };
 
 /* Precision of the gather in the model kernels. FP64 is the drop-in (parity)
  * form; FP32_SPLIT gathers an FP32 coefficient copy at a height split into

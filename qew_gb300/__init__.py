@@ -40,7 +40,7 @@ from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # n
                     QEW_FIELD_SINCOS, QEW_FIELD_WASHBOARD, QEW_FIELD_ZERO,
                     QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT, QEW_PREC_FP32_SPLIT,
                     QEW_PREC_FP64, QEW_RK_PLAIN, QEW_RK_RESIDENT, QEW_STORE_FP32,
-                    QEW_STORE_FP64, QewError)
+                    QEW_STORE_FP32_EDGE, QEW_STORE_FP64, QewError)
 
 __all__ = [
     "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
@@ -211,7 +211,9 @@ class FilteredNoise(_Noise):
     ``field`` is the real-space field in the reference's host layout
     ``field[i, j]`` (i along x, j along y), as a numpy array or a CUDA tensor.
     The periodic cubic B-spline prefilter runs on the GPU. ``store`` selects
-    FP64 and/or FP32 coefficient storage.
+    FP64 and/or FP32 coefficient storage; QEW_STORE_FP32_EDGE (with FP32) adds
+    the x-filtered copy that the split-form gradient reads on a line with one
+    point per field column (4 taps per edge instead of 16).
     """
 
     kind = QEW_FIELD_BSPLINE

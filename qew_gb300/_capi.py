@@ -27,7 +27,7 @@ QEW_ERR_UNSUPPORTED = 6
 
 QEW_FIELD_BSPLINE, QEW_FIELD_ZERO, QEW_FIELD_CONST = 0, 1, 2
 QEW_FIELD_HARMONIC, QEW_FIELD_WASHBOARD, QEW_FIELD_SINCOS = 3, 4, 5
-QEW_STORE_FP64, QEW_STORE_FP32 = 1, 2
+QEW_STORE_FP64, QEW_STORE_FP32, QEW_STORE_FP32_EDGE = 1, 2, 4
 QEW_PREC_FP64, QEW_PREC_FP32_SPLIT = 0, 1
 QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
 QEW_NOALLOC_MAX_N = 1048576

@@ -107,6 +107,24 @@ __global__ void k_to_fp32(const double *__restrict__ in, float *__restrict__ out
         out[k] = (float)in[k];
 }
 
+// E[j][e] = sum_a w_a(1/2) c[j][(e - 1 + a) mod nx], FP64 sum rounded once to
+// FP32: the x part of the cubic B-spline sum (filtered_noise.h:33-44 at t = 1/2,
+// where the weights are 1/48, 23/48, 23/48, 1/48) at the midpoint of every
+// column pair; c is [ny][nx], x fastest.
+__global__ void k_edge_fp32(const double *__restrict__ c, float *__restrict__ out, int nx,
+                            size_t n) {
+    const double w0 = 1.0 / 48.0, w1 = 23.0 / 48.0;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
+         k += (size_t)gridDim.x * blockDim.x) {
+        const int e = (int)(k % (size_t)nx);
+        const double *row = c + (k - (size_t)e);
+        const int em = (e == 0) ? nx - 1 : e - 1;
+        const int ep = (e + 1 == nx) ? 0 : e + 1;
+        const int ep2 = (ep + 1 == nx) ? 0 : ep + 1;
+        out[k] = (float)(w0 * row[em] + w1 * row[e] + w1 * row[ep] + w0 * row[ep2]);
+    }
+}
+
 template <class Noise>
 __global__ void k_sample(Noise nz, const double *__restrict__ x, const double *__restrict__ y,
                          int m, double *v, double *dvdx, double *dvdy) {
@@ -213,6 +231,8 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
     if (!ctx || !out || !src || nx <= 0 || ny <= 0 || !(Lx > 0) || !(Ly > 0) ||
         (store & (QEW_STORE_FP64 | QEW_STORE_FP32)) == 0)
         return qew_fail(ctx, QEW_ERR_INVALID, "field_create: bad arguments");
+    if ((store & QEW_STORE_FP32_EDGE) && !(store & QEW_STORE_FP32))
+        return qew_fail(ctx, QEW_ERR_INVALID, "field_create: QEW_STORE_FP32_EDGE needs QEW_STORE_FP32");
     // transposes tile 32 columns per grid row: keep both extents within the grid limit
     if (nx > 65535 * 32 || ny > 65535 * 32)
         return qew_fail(ctx, QEW_ERR_INVALID, "field_create: nx and ny must be <= %d", 65535 * 32);
@@ -235,6 +255,7 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
         qew_free_async(tmp, ctx->stream);
         qew_free_async(c64, ctx->stream);
         qew_free_async(f->coef32, ctx->stream);
+        qew_free_async(f->edge32, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
         delete f;
         return s;
@@ -263,6 +284,13 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
         const int blocks = ctx->num_sms * 8;
         k_to_fp32<<<blocks, 256, 0, ctx->stream>>>(c64, f->coef32, N);
         st = qew_launch_check(ctx, "to_fp32");
+        if (st != QEW_OK) return cleanup(st);
+    }
+    if (store & QEW_STORE_FP32_EDGE) {
+        if (qew_alloc_async(ctx, (void **)&f->edge32, N * sizeof(float)) != QEW_OK)
+            return cleanup(QEW_ERR_NOMEM);
+        k_edge_fp32<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(c64, f->edge32, nx, N);
+        st = qew_launch_check(ctx, "edge_fp32");
         if (st != QEW_OK) return cleanup(st);
     }
     e = cudaStreamSynchronize(ctx->stream);
@@ -430,10 +458,12 @@ qew_status qew_field_destroy(qew_field *f) {
     if (!f) return QEW_OK;
     cudaSetDevice(f->device);
     // the coefficients may be in use on any stream: wait for the device
-    if (f->coef64 || f->coef32) cudaDeviceSynchronize();
+    const bool held = f->coef64 || f->coef32 || f->edge32;
+    if (held) cudaDeviceSynchronize();
     qew_free_async(f->coef64, f->stream);
     qew_free_async(f->coef32, f->stream);
-    if (f->coef64 || f->coef32) cudaStreamSynchronize(f->stream);
+    qew_free_async(f->edge32, f->stream);
+    if (held) cudaStreamSynchronize(f->stream);
     delete f;
     return QEW_OK;
 }
@@ -444,6 +474,7 @@ void qew_field_release_on(qew_field *f, cudaStream_t stream) {
     if (!f) return;
     qew_free_async(f->coef64, stream);
     qew_free_async(f->coef32, stream);
+    qew_free_async(f->edge32, stream);
     delete f;
 }
 

@@ -53,6 +53,7 @@ struct qew_field {
     double p0 = 0, p1 = 0, p2 = 0;
     double *coef64 = nullptr;  // [ny][nx], x fastest
     float *coef32 = nullptr;   // [ny][nx], x fastest
+    float *edge32 = nullptr;   // [ny][nx]: coefficients filtered along x at e + 1/2
     cudaStream_t stream = nullptr;  // stream the coefficients were allocated on
 };
 

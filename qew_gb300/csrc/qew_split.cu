@@ -9,7 +9,11 @@
 //     exact integer cell sums plus FP32 fraction sums,
 //   * edge x positions from integer arithmetic when the line and the field
 //     share their resolution and length (gx = e + 1/2 exactly), FP64 only in
-//     the general case.
+//     the general case,
+//   * on such a shared grid, when the field holds the x-filtered store
+//     (QEW_STORE_FP32_EDGE), the x half of the stencil sum read as one
+//     precomputed value per row: 4 taps per edge instead of 16, the same
+//     rows and so the same DRAM bytes, a quarter of the load instructions.
 // Error against the FP64 form is FP32 rounding of the field, weights and sums
 // (about 1e-6 of the gradient's scale; the tests state the bound).
 #include <cmath>
@@ -114,6 +118,32 @@ __device__ __forceinline__ float split_dvdy_interior(const float *__restrict__ c
     return dg * inv_dy;
 }
 
+// dV/dy at the midpoint of edge e on a shared grid from the x-filtered store
+// E (E[j][e] = sum_a w_a(1/2) c[j][e - 1 + a]): the remaining sum over the 4
+// stencil rows, one tap each. The interior form (1 <= cy <= ny - 3) indexes
+// from one base pointer; the other wraps the rows.
+__device__ __forceinline__ float split_dvdy_edge_interior(const float *__restrict__ E, int nx,
+                                                          int e, int cy, float fy, float inv_dy) {
+    float dwy[4];
+    bsw_deriv_f(fy, dwy);
+    const float *p = E + ((size_t)(cy - 1) * (size_t)nx + (size_t)e);
+    float dg = 0.0f;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) dg += dwy[b] * __ldg(p + (size_t)b * (size_t)nx);
+    return dg * inv_dy;
+}
+__device__ __forceinline__ float split_dvdy_edge(const float *__restrict__ E, int nx, int ny,
+                                                 int e, int cy, float fy, float inv_dy) {
+    int ys[4];
+    wrap4(wrap_cell(cy, ny), ny, ys);
+    float dwy[4];
+    bsw_deriv_f(fy, dwy);
+    float dg = 0.0f;
+#pragma unroll
+    for (int b = 0; b < 4; ++b) dg += dwy[b] * __ldg(E + (size_t)ys[b] * (size_t)nx + (size_t)e);
+    return dg * inv_dy;
+}
+
 // Midpoint of two split heights: (c0 + f0 + c1 + f1) / 2 as (cell, frac).
 __device__ __forceinline__ void split_mid(int c0, float f0, int c1, float f1, int &cm, float &fm) {
     const int C = c0 + c1;
@@ -182,21 +212,29 @@ k_gradient_split(const double *__restrict__ h64, const int *__restrict__ hc,
     float wx_half[4];  // x weights at fx = 1/2, every edge but the wrap edge on a shared grid
     bsw_value_f(0.5f, wx_half);
     auto edge = [&](int e, int sl, int sr, int out) {
-        int ix, cm;
-        float fx, fm;
-        edge_x(g, e, ix, fx);
+        int cm;
+        float fm;
         split_mid(s_c[sl], s_f[sl], s_c[sr], s_f[sr], cm, fm);
-        if (ix >= 1 && ix <= g.nx - 3 && cm >= 1 && cm <= g.ny - 3) {
-            float wx[4];
-            if (g.same_grid && e + 1 < n) {
-#pragma unroll
-                for (int a = 0; a < 4; ++a) wx[a] = wx_half[a];
-            } else {
-                bsw_value_f(fx, wx);
-            }
-            s_dv[out] = split_dvdy_interior(g.coef, g.nx, ix, wx, cm, fm, g.inv_dy_f);
+        const bool y_inner = (cm >= 1 && cm <= g.ny - 3);
+        if (g.edge && e + 1 < n) {  // x-filtered store: 4 taps (the wrap edge sits at (n-1)/2)
+            s_dv[out] = y_inner ? split_dvdy_edge_interior(g.edge, g.nx, e, cm, fm, g.inv_dy_f)
+                                : split_dvdy_edge(g.edge, g.nx, g.ny, e, cm, fm, g.inv_dy_f);
         } else {
-            s_dv[out] = split_dvdy(g.coef, g.nx, g.ny, ix, fx, cm, fm, g.inv_dy_f);
+            int ix;
+            float fx;
+            edge_x(g, e, ix, fx);
+            if (y_inner && ix >= 1 && ix <= g.nx - 3) {
+                float wx[4];
+                if (g.same_grid && e + 1 < n) {
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) wx[a] = wx_half[a];
+                } else {
+                    bsw_value_f(fx, wx);
+                }
+                s_dv[out] = split_dvdy_interior(g.coef, g.nx, ix, wx, cm, fm, g.inv_dy_f);
+            } else {
+                s_dv[out] = split_dvdy(g.coef, g.nx, g.ny, ix, fx, cm, fm, g.inv_dy_f);
+            }
         }
         if (arc) {
             const float dh = ((float)(s_c[sr] - s_c[sl]) + (s_f[sr] - s_f[sl])) * g.dy_over_dx;
@@ -255,6 +293,7 @@ SplitGeom qew_split_geom(const qew_field *f, int n, const qew_params *p) {
     g.nx = f->nx;
     g.ny = f->ny;
     g.same_grid = (n == f->nx && p->physical_size == f->Lx) ? 1 : 0;
+    g.edge = g.same_grid ? f->edge32 : nullptr;
     g.half_ratio = 0.5 * (p->physical_size / n) / f->dx;
     g.dy = f->dy;
     g.inv_dy = 1.0 / f->dy;

@@ -5,6 +5,7 @@
 
 struct SplitGeom {
     const float *coef;  // [ny][nx] FP32 coefficients
+    const float *edge;  // [ny][nx] x-filtered at e + 1/2 when same_grid and stored, else null
     int n, nx, ny;
     int same_grid;      // n == nx and physical_size == Lx: gx = e + 1/2 exactly
     double half_ratio;  // 0.5 * (physical_size / n) / dx_field (general case)

@@ -69,23 +69,84 @@ def test_split_join_roundtrip(Q):
 
 
 def test_split_full_size(Q, O):
-    """L = 2^20 on a 2^20 x 64 field against the OpenMP oracle."""
+    """L = 2^20 on a 2^20 x 64 field against the OpenMP oracle, with and
+    without the x-filtered store."""
     import torch
     n, ny = 1 << 20, 64
     fld = np.random.default_rng(3).standard_normal((n, ny))
-    f = Q.FilteredNoise(fld, float(n), float(ny), store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    f = Q.FilteredNoise(fld, float(n), float(ny),
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | Q.QEW_STORE_FP32_EDGE)
     of = O.BSplineField(fld, float(n), float(ny), coef=f.coefficients())
     rng = np.random.default_rng(4)
     h = 32 + np.cumsum(rng.standard_normal(n)) * 0.02
     po = O.params(float(n), 1.0, 0.1, 0)
     go = O.gradient(h, po, of, omp=True)
-    cell, frac = Q.split_heights(t64(h), f)
-    g = npy(Q.gradient_split(cell, frac, Q.Params(float(n), 1.0, 0.1), f)).astype(np.float64)
     g_el = O.gradient(h, po, O.ZeroNoise(), omp=True)
     scale = max(np.max(np.abs(g_el)), np.max(np.abs(go - g_el)))
+    p = Q.Params(float(n), 1.0, 0.1)
+    cell, frac = Q.split_heights(t64(h), f)
+    g = npy(Q.gradient_split(cell, frac, p, f)).astype(np.float64)
     assert np.max(np.abs(g - go)) <= TOL * scale
     del f
     torch.cuda.empty_cache()
+    f16 = Q.FilteredNoise(fld, float(n), float(ny), store=Q.QEW_STORE_FP32)
+    g16 = npy(Q.gradient_split(cell, frac, p, f16)).astype(np.float64)
+    assert np.max(np.abs(g16 - go)) <= TOL * scale
+    del f16
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("n, ny, rough", [
+    (4096, 64, 0.2),    # smooth line, interior rows
+    (4096, 16, 30.0),   # rough line wrapping the rows many times
+    (1001, 24, 1.0),    # odd n: the wrap edge sits at x = (n-1)/2 exactly (fx = 0)
+    (1000, 4, 0.5),     # four rows: every stencil wraps in y
+])
+def test_split_edge_store_error_bound(Q, O, model, n, ny, rough):
+    """The x-filtered store (4 taps per edge) meets the same bound against the
+    FP64 oracle as the 16-tap form, and the two FP32 forms agree to it."""
+    Lx = float(n)
+    fld = gaussian_field(n, ny, 3.0, n + 7 * ny)
+    fe = Q.FilteredNoise(fld, Lx, float(ny),
+                         store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | Q.QEW_STORE_FP32_EDGE)
+    f16 = Q.FilteredNoise(fld, Lx, float(ny), store=Q.QEW_STORE_FP32)
+    of = O.BSplineField(fld, Lx, float(ny), coef=fe.coefficients())
+    rng = np.random.default_rng(n * ny)
+    h = ny / 2 + np.cumsum(rng.standard_normal(n)) * rough * 0.1 + 0.3 * ny * np.sin(
+        np.linspace(0, 2 * np.pi, n, endpoint=False))
+    p = Q.Params(Lx, 0.9, 0.02, Q.Model(model))
+    po = O.params(Lx, 0.9, 0.02, model)
+    go = O.gradient(h, po, of)
+    scale = term_scale(O, h, po, of)
+    cell, frac = Q.split_heights(t64(h), fe)
+    ge = npy(Q.gradient_split(cell, frac, p, fe)).astype(np.float64)
+    g16 = npy(Q.gradient_split(cell, frac, p, f16)).astype(np.float64)
+    assert np.max(np.abs(ge - go)) <= TOL * scale
+    assert np.max(np.abs(ge - g16)) <= TOL * scale
+    # FP64 heights in: the same kernel splits them itself
+    g64 = npy(Q.gradient(t64(h), p, fe, precision=Q.QEW_PREC_FP32_SPLIT)).astype(np.float32)
+    assert np.array_equal(g64.astype(np.float64), ge)
+
+
+def test_split_edge_store_ignored_off_grid(Q):
+    """A line whose points do not match the field columns uses the 16-tap form:
+    the x-filtered store changes nothing there."""
+    nx, ny, n = 2048, 48, 3000
+    fld = gaussian_field(nx, ny, 3.0, 5)
+    fe = Q.FilteredNoise(fld, float(nx), float(ny), store=Q.QEW_STORE_FP32 | Q.QEW_STORE_FP32_EDGE)
+    f16 = Q.FilteredNoise(fld, float(nx), float(ny), store=Q.QEW_STORE_FP32)
+    h = t64(ny / 2 + np.cumsum(np.random.default_rng(2).standard_normal(n)) * 0.05)
+    p = Q.Params(float(nx), 1.0, 0.0)
+    cell, frac = Q.split_heights(h, fe)
+    assert np.array_equal(npy(Q.gradient_split(cell, frac, p, fe)),
+                          npy(Q.gradient_split(cell, frac, p, f16)))
+
+
+def test_edge_store_needs_fp32(Q):
+    with pytest.raises(ValueError, match="FP32_EDGE"):
+        Q.FilteredNoise(gaussian_field(64, 16, 3.0, 1), 64.0, 16.0,
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32_EDGE)
 
 
 def test_split_needs_fp32_storage(Q):
