@@ -28,6 +28,7 @@ constexpr int kEnsBS = 512;
 struct EnsJob {
     const double *coef64;
     const float *coef32;
+    const float *edge32;
     int nx, ny;
     double fdx, fdy, Lx;
     double *h;
@@ -67,6 +68,7 @@ __device__ __forceinline__ NoiseSplit32 job_noise32(const EnsJob &j) {
     nz.dx_pow2 = dbl_is_pow2(j.fdx);
     nz.dy_pow2 = dbl_is_pow2(j.fdy);
     nz.xconst = (j.n == j.nx && j.p.physical_size == j.Lx && nz.dx_pow2);
+    nz.edge = nz.xconst ? j.edge32 : nullptr;
     nz.inv_dy_f = (float)(1.0 / j.fdy);
     return nz;
 }
@@ -126,6 +128,7 @@ extern "C" qew_status qew_ensemble_minimize(qew_ctx *ctx, int count, const qew_e
         EnsJob &j = jobs[k];
         j.coef64 = f->coef64;
         j.coef32 = f->coef32;
+        j.edge32 = f->edge32;
         j.nx = f->nx;
         j.ny = f->ny;
         j.fdx = f->dx;

@@ -2,7 +2,10 @@
 // interface, for solvers that run their first iterations on FP32
 // coefficients: the height is split into an integer cell and an FP32
 // fraction (the only FP64 work is that split), the weights and the 16-tap
-// sum are FP32, and the result is widened back to FP64.
+// sum are FP32, and the result is widened back to FP64. On a line with one
+// point per field column, a field holding the x-filtered store (the x half of
+// the stencil sum at every column midpoint) serves the edge midpoints with 4
+// taps instead of 16.
 #pragma once
 
 #include "qew_internal.cuh"
@@ -25,6 +28,7 @@ __device__ __forceinline__ void bsw_deriv32(float t, float dw[4]) {
 
 struct NoiseSplit32 {
     const float *__restrict__ coef;  // [ny][nx] FP32
+    const float *__restrict__ edge;  // [ny][nx] x-filtered at e + 1/2 (xconst lines), or null
     int nx, ny;
     double dx, dy, inv_dx, inv_dy;
     bool dx_pow2, dy_pow2;
@@ -74,6 +78,26 @@ struct NoiseSplit32 {
         }
         return acc;
     }
+    // The column sum at the midpoint of edge e from the x-filtered store.
+    __device__ __forceinline__ float taps_edge(int e, int iy, float fy, bool deriv) const {
+        float wy[4];
+        if (deriv)
+            bsw_deriv32(fy, wy);
+        else
+            bsw_value32(fy, wy);
+        float acc = 0.0f;
+        if (iy >= 1 && iy <= ny - 3) {
+            const float *p = edge + ((size_t)(iy - 1) * (size_t)nx + (size_t)e);
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc += wy[b] * __ldg(p + (size_t)b * (size_t)nx);
+            return acc;
+        }
+        int ys[4];
+        wrap4(iy, ny, ys);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc += wy[b] * __ldg(edge + (size_t)ys[b] * (size_t)nx + (size_t)e);
+        return acc;
+    }
     __device__ __forceinline__ double value(double x, double y) const {
         int ix, iy;
         float fx, fy;
@@ -93,14 +117,15 @@ struct NoiseSplit32 {
         int iy;
         float fy;
         loc_y(y, iy, fy);
-        return (double)taps(e, 0.5f, iy, fy, false);
+        return (double)(edge ? taps_edge(e, iy, fy, false) : taps(e, 0.5f, iy, fy, false));
     }
     __device__ __forceinline__ double dvdy_edge(int e, double xc, double y) const {
         if (!xconst || e + 1 >= nx) return dvdy(xc, y);
         int iy;
         float fy;
         loc_y(y, iy, fy);
-        return (double)(taps(e, 0.5f, iy, fy, true) * inv_dy_f);
+        const float t = edge ? taps_edge(e, iy, fy, true) : taps(e, 0.5f, iy, fy, true);
+        return (double)(t * inv_dy_f);
     }
     __device__ __forceinline__ void sample(double x, double y, double &v, double &a,
                                            double &b) const {
@@ -131,6 +156,7 @@ static inline NoiseSplit32 make_split32(const qew_field *f, int n, double physic
     nz.dx_pow2 = qew_is_pow2(f->dx);
     nz.dy_pow2 = qew_is_pow2(f->dy);
     nz.xconst = (n > 0 && n == f->nx && physical_size == f->Lx && nz.dx_pow2);
+    nz.edge = nz.xconst ? f->edge32 : nullptr;
     nz.inv_dy_f = (float)(1.0 / f->dy);
     return nz;
 }

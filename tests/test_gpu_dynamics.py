@@ -139,10 +139,12 @@ def test_resident_run_matches_step_loop(Q, model):
     assert np.max(np.abs(a - b)) <= 1e-12 * np.max(np.abs(a))
 
 
-def test_resident_run_fp32(Q):
-    """FP32-gather run: deterministic part close to FP64, FP32 normals N(0,1)."""
+@pytest.mark.parametrize("edge", [False, True])
+def test_resident_run_fp32(Q, edge):
+    """FP32-gather run (16 taps, or 4 from the x-filtered store): deterministic
+    part close to FP64, FP32 normals N(0,1)."""
     n, ny = 4096, 64
-    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | (Q.QEW_STORE_FP32_EDGE if edge else 0)
     f = Q.FilteredNoise(band_limited_field(n, ny, float(n), float(ny), 1.0, 4.0, 8),
                         float(n), float(ny), store=store)
     p = Q.Params(float(n), 1.0, 0.2, Q.Model.Arclength)

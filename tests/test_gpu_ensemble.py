@@ -39,10 +39,10 @@ def test_generated_field_statistics(Q):
     assert abs(corr - np.exp(-r * r / (4 * xi * xi))) < 0.1
 
 
-def _c3_lines(Q, count, seed, lmin=256, lmax=2048):
+def _c3_lines(Q, count, seed, lmin=256, lmax=2048, edge=False):
     rng = np.random.default_rng(seed)
     lines = []
-    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | (Q.QEW_STORE_FP32_EDGE if edge else 0)
     for k in range(count):
         L = int(round(np.exp(rng.uniform(np.log(lmin), np.log(lmax))) / 2)) * 2
         xi = rng.uniform(2, 8)
@@ -53,9 +53,9 @@ def _c3_lines(Q, count, seed, lmin=256, lmax=2048):
     return lines
 
 
-@pytest.mark.parametrize("ftol32", [0.0, 2e-5])
-def test_ensemble_reaches_fp64_tolerance(Q, ftol32):
-    lines = _c3_lines(Q, 48, 3)
+@pytest.mark.parametrize("ftol32, edge", [(0.0, False), (2e-5, False), (2e-5, True)])
+def test_ensemble_reaches_fp64_tolerance(Q, ftol32, edge):
+    lines = _c3_lines(Q, 48, 3, edge=edge)
     lp = Q.LbfgsParams(m=10, ftol=FTOL, max_iter=20000, precondition=True, ls_fallback=True)
     res = Q.ensemble_minimize(lines, lp, ftol_fp32=ftol32)
     for (h, p, f, _), r in zip(lines, res):
