@@ -111,17 +111,17 @@ __global__ void k_to_fp32(const double *__restrict__ in, float *__restrict__ out
 // FP32: the x part of the cubic B-spline sum (filtered_noise.h:33-44 at t = 1/2,
 // where the weights are 1/48, 23/48, 23/48, 1/48) at the midpoint of every
 // column pair; c is [ny][nx], x fastest.
-__global__ void k_edge_fp32(const double *__restrict__ c, float *__restrict__ out, int nx,
-                            size_t n) {
+__global__ void k_edge_fp32(const double *__restrict__ c, float *__restrict__ out, int nx, int ny) {
     const double w0 = 1.0 / 48.0, w1 = 23.0 / 48.0;
-    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n;
-         k += (size_t)gridDim.x * blockDim.x) {
-        const int e = (int)(k % (size_t)nx);
-        const double *row = c + (k - (size_t)e);
-        const int em = (e == 0) ? nx - 1 : e - 1;
-        const int ep = (e + 1 == nx) ? 0 : e + 1;
-        const int ep2 = (ep + 1 == nx) ? 0 : ep + 1;
-        out[k] = (float)(w0 * row[em] + w1 * row[e] + w1 * row[ep] + w0 * row[ep2]);
+    for (int j = blockIdx.y; j < ny; j += gridDim.y) {
+        const double *row = c + (size_t)j * (size_t)nx;
+        float *o = out + (size_t)j * (size_t)nx;
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nx; e += gridDim.x * blockDim.x) {
+            const int em = (e == 0) ? nx - 1 : e - 1;
+            const int ep = (e + 1 == nx) ? 0 : e + 1;
+            const int ep2 = (ep + 1 == nx) ? 0 : ep + 1;
+            o[e] = (float)(w0 * row[em] + w1 * row[e] + w1 * row[ep] + w0 * row[ep2]);
+        }
     }
 }
 
@@ -289,7 +289,8 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
     if (store & QEW_STORE_FP32_EDGE) {
         if (qew_alloc_async(ctx, (void **)&f->edge32, N * sizeof(float)) != QEW_OK)
             return cleanup(QEW_ERR_NOMEM);
-        k_edge_fp32<<<ctx->num_sms * 8, 256, 0, ctx->stream>>>(c64, f->edge32, nx, N);
+        const dim3 eg((unsigned)std::min((nx + 255) / 256, 64), (unsigned)std::min(ny, 65535));
+        k_edge_fp32<<<eg, 256, 0, ctx->stream>>>(c64, f->edge32, nx, ny);
         st = qew_launch_check(ctx, "edge_fp32");
         if (st != QEW_OK) return cleanup(st);
     }

@@ -143,6 +143,34 @@ def test_split_edge_store_ignored_off_grid(Q):
                           npy(Q.gradient_split(cell, frac, p, f16)))
 
 
+@pytest.mark.parametrize("n, count", [(5000, 5), (150001, 9)])
+def test_split_edge_store_batch(Q, O, n, count):
+    """Batched lines on the x-filtered store (the persistent launch: a ragged
+    last tile; at 150001 x 9 more tiles than resident CTAs, so CTAs loop):
+    bitwise equal to one line per call, and within the bound of the oracle."""
+    import torch
+    ny = 48
+    fld = gaussian_field(n, ny, 3.0, 17)
+    f = Q.FilteredNoise(fld, float(n), float(ny),
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | Q.QEW_STORE_FP32_EDGE)
+    of = O.BSplineField(fld, float(n), float(ny), coef=f.coefficients())
+    rng = np.random.default_rng(n + count)
+    hs = [ny / 2 + np.cumsum(rng.standard_normal(n)) * 0.1 for _ in range(count)]
+    sp = [Q.split_heights(t64(h), f) for h in hs]
+    cells = torch.stack([c for c, _ in sp]).contiguous()
+    fracs = torch.stack([fr for _, fr in sp]).contiguous()
+    for model in (0, 1):
+        p = Q.Params(float(n), 0.8, 0.05, Q.Model(model))
+        po = O.params(float(n), 0.8, 0.05, model)
+        gb = npy(Q.gradient_split_batch(cells, fracs, p, f))
+        for k in (0, count // 2, count - 1):
+            assert np.array_equal(gb[k], npy(Q.gradient_split(sp[k][0], sp[k][1], p, f)))
+            go = O.gradient(hs[k], po, of, omp=True)
+            g_el = O.gradient(hs[k], po, O.ZeroNoise(), omp=True)
+            scale = max(np.max(np.abs(g_el)), np.max(np.abs(go - g_el)))
+            assert np.max(np.abs(gb[k].astype(np.float64) - go)) <= TOL * scale
+
+
 def test_edge_store_needs_fp32(Q):
     with pytest.raises(ValueError, match="FP32_EDGE"):
         Q.FilteredNoise(gaussian_field(64, 16, 3.0, 1), 64.0, 16.0,
