@@ -50,6 +50,10 @@ def parse():
     ap.add_argument("--small", action="store_true",
                     help="small case for profiling: the same batched launch (8 lines of "
                          "L=2^20) on a 256-row field (3 GB of coefficients)")
+    ap.add_argument("--no-edge-store", action="store_true",
+                    help="field without the x-filtered FP32 copy: the split gather reads the 16 "
+                         "B-spline taps per edge (the form used on lines that do not have one "
+                         "point per field column)")
     ap.add_argument("--profile-run", action="store_true",
                     help="GPU timed loop only (no e2e, CPU baseline or clock sampling)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -632,8 +636,9 @@ def run_ours(args):
     else:
         L, ny, n_inst = L_FULL, NY_FULL, N_INST
     field = gaussian_field_gpu(torch, L, ny, XI, SEED + rank)
+    edge = 0 if args.no_edge_store else Q.QEW_STORE_FP32_EDGE
     noise = Q.FilteredNoise(field, float(L), float(ny),
-                            store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | Q.QEW_STORE_FP32_EDGE)
+                            store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | edge)
     del field
     torch.cuda.empty_cache()
     rng = np.random.default_rng(SEED + 1000 * rank)
@@ -696,19 +701,25 @@ def run_ours(args):
                 "launch_us": launch_ms * 1e3, "peak_source": peak_kind}
 
     roof_split = roofline(t_ms if headline_split else t2_ms,
-                          launches if headline_split else launches2, 28.0, "k_gradient_split")
+                          launches if headline_split else launches2, 28.0,
+                          "k_gradient_split" if args.no_edge_store else "k_gradient_split_persist")
     roof_fp64 = roofline(t2_ms if headline_split else t_ms,
                          launches2 if headline_split else launches, 48.0, "k_gradient")
-    roof_split["field_store"] = ("FP32 coefficients plus the x-filtered copy: 4 taps per edge "
-                                 "(the same rows, so the same DRAM bytes, as 16 taps)")
+    roof_split["field_store"] = (
+        "FP32 coefficients: 16 taps per edge" if args.no_edge_store else
+        "FP32 coefficients plus the x-filtered copy: 4 taps per edge (the same rows, so the "
+        "same DRAM bytes, as 16 taps)")
     # DRAM bytes (read + write) per line point from one ncu capture of each
     # kernel: the split gather's batched launch (8 lines of 2^20 points, 256-row
-    # field: 241.858816 MB read + 20.879104 MB written) and the FP64 gather on
+    # field: 237.687808 MB read + 23.139072 MB written with the x-filtered store,
+    # 241.858816 + 20.879104 MB with 16 taps per edge) and the FP64 gather on
     # one 2^20-point line (53.188352 MB), scaled to the points of one launch
     # (traffic grows in proportion to the points).
     pts_split = args.steps * n_inst * L / max(launches if headline_split else launches2, 1)
     pts_fp64 = args.steps * n_inst * L / max(launches2 if headline_split else launches, 1)
-    roof_split["traffic"] = (241.858816e6 + 20.879104e6) / (8 * L_FULL) * pts_split
+    split_bytes = ((241.858816e6 + 20.879104e6) if args.no_edge_store else
+                   (237.687808e6 + 23.139072e6))
+    roof_split["traffic"] = split_bytes / (8 * L_FULL) * pts_split
     roof_fp64["traffic"] = 53.188352e6 / L_FULL * pts_fp64
 
     e2e = None
