@@ -161,7 +161,9 @@ __device__ __forceinline__ void split_mid(int c0, float f0, int c1, float f1, in
 
 // Edge e of a tile, between height slots `slot` and `slot + 1`: writes dV/dy
 // at the edge midpoint to dv[slot] and, for the arclength model, the slope
-// term s / sqrt(1 + s^2) to sl[slot].
+// term s / sqrt(1 + s^2) to sl[slot]. kStore: the caller guarantees g.edge
+// (the x-filtered store applies), so only the wrap edge takes the general path.
+template <bool kStore>
 __device__ __forceinline__ void split_edge(const SplitGeom &g, const float wx_half[4], int e,
                                            const int *sc, const float *sf, int slot, float *dv,
                                            float *sl) {
@@ -169,7 +171,7 @@ __device__ __forceinline__ void split_edge(const SplitGeom &g, const float wx_ha
     float fm;
     split_mid(sc[slot], sf[slot], sc[slot + 1], sf[slot + 1], cm, fm);
     const bool y_inner = (cm >= 1 && cm <= g.ny - 3);
-    if (g.edge && e + 1 < g.n) {  // x-filtered store: 4 taps (the wrap edge sits at (n-1)/2)
+    if ((kStore || g.edge) && e + 1 < g.n) {  // x-filtered store: 4 taps (the wrap edge sits at (n-1)/2)
         dv[slot] = y_inner ? split_dvdy_edge_interior(g.edge, g.nx, e, cm, fm, g.inv_dy_f)
                            : split_dvdy_edge(g.edge, g.nx, g.ny, e, cm, fm, g.inv_dy_f);
     } else {
@@ -266,9 +268,10 @@ k_gradient_split(const double *__restrict__ h64, const int *__restrict__ hc,
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
         const int j = t + k * kBS;
-        if (j < cnt) split_edge(g, wx_half, base + j, s_c, s_f, j + 1, s_dv, s_sl);
+        if (j < cnt) split_edge<false>(g, wx_half, base + j, s_c, s_f, j + 1, s_dv, s_sl);
     }
-    if (t == kBS - 1) split_edge(g, wx_half, base == 0 ? n - 1 : base - 1, s_c, s_f, 0, s_dv, s_sl);
+    if (t == kBS - 1)
+        split_edge<false>(g, wx_half, base == 0 ? n - 1 : base - 1, s_c, s_f, 0, s_dv, s_sl);
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
@@ -305,11 +308,13 @@ k_gradient_split_persist(const int *__restrict__ hc, const float *__restrict__ h
     __shared__ float s_sl[kTile + 1];
     const int n = g.n;
     const int per_line = (n + kTile - 1) / kTile;
-    const int tiles = per_line * count;
     const int t = threadIdx.x;
-    auto fetch = [&](int tile, int buf) {  // heights of `tile` (+ halo) into buffer buf
-        const int line = tile / per_line;
-        const int base = (tile - line * per_line) * kTile;
+    // This CTA's tiles are blockIdx.x + k * gridDim.x in line-major order;
+    // their (line, index in line) advance by a fixed step, one division per CTA.
+    const int step_l = (int)gridDim.x / per_line;
+    const int step_i = (int)gridDim.x - step_l * per_line;
+    auto fetch = [&](int line, int idx, int buf) {  // heights of a tile (+ halo) into buffer buf
+        const int base = idx * kTile;
         const int cnt = min(kTile, n - base);
         const int *c = hc + (size_t)line * (size_t)n;
         const float *f = hf + (size_t)line * (size_t)n;
@@ -334,11 +339,16 @@ k_gradient_split_persist(const int *__restrict__ hc, const float *__restrict__ h
     };
     float wx_half[4];
     bsw_value_f(0.5f, wx_half);
-    int tile = blockIdx.x;
-    if (tile < tiles) fetch(tile, 0);
-    for (int buf = 0; tile < tiles; tile += gridDim.x, buf ^= 1) {
-        const int line = tile / per_line;
-        const int base = (tile - line * per_line) * kTile;
+    int line = (int)blockIdx.x / per_line;
+    int idx = (int)blockIdx.x - line * per_line;
+    if (line < count) fetch(line, idx, 0);
+    for (int buf = 0; line < count; buf ^= 1) {
+        int nline = line + step_l, nidx = idx + step_i;
+        if (nidx >= per_line) {
+            nidx -= per_line;
+            ++nline;
+        }
+        const int base = idx * kTile;
         const int cnt = min(kTile, n - base);
         const int *sc = s_c[buf];
         const float *sf = s_f[buf];
@@ -347,13 +357,14 @@ k_gradient_split_persist(const int *__restrict__ hc, const float *__restrict__ h
         // and every thread has left the previous tile, whose buffer (the
         // other one) may now be refilled and whose edges may be rewritten.
         __syncthreads();
-        if (tile + (int)gridDim.x < tiles) fetch(tile + gridDim.x, buf ^ 1);
+        if (nline < count) fetch(nline, nidx, buf ^ 1);
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             const int j = t + k * kBS;
-            if (j < cnt) split_edge(g, wx_half, base + j, sc, sf, j + 1, s_dv, s_sl);
+            if (j < cnt) split_edge<true>(g, wx_half, base + j, sc, sf, j + 1, s_dv, s_sl);
         }
-        if (t == kBS - 1) split_edge(g, wx_half, base == 0 ? n - 1 : base - 1, sc, sf, 0, s_dv, s_sl);
+        if (t == kBS - 1)
+            split_edge<true>(g, wx_half, base == 0 ? n - 1 : base - 1, sc, sf, 0, s_dv, s_sl);
         __syncthreads();  // barrier B: edges done
         float *out = grad + (size_t)line * (size_t)n + base;
 #pragma unroll
@@ -362,6 +373,8 @@ k_gradient_split_persist(const int *__restrict__ hc, const float *__restrict__ h
             if (j >= cnt) break;
             __stcs(out + j, split_site(g, sc, sf, s_dv, s_sl, j));
         }
+        line = nline;
+        idx = nidx;
     }
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
