@@ -711,14 +711,14 @@ def run_ours(args):
         "same DRAM bytes, as 16 taps)")
     # DRAM bytes (read + write) per line point from one ncu capture of each
     # kernel: the split gather's batched launch (8 lines of 2^20 points, 256-row
-    # field: 237.687808 MB read + 23.139072 MB written with the x-filtered store,
+    # field: 237.686784 MB read + 22.566656 MB written with the x-filtered store,
     # 241.858816 + 20.879104 MB with 16 taps per edge) and the FP64 gather on
     # one 2^20-point line (53.188352 MB), scaled to the points of one launch
     # (traffic grows in proportion to the points).
     pts_split = args.steps * n_inst * L / max(launches if headline_split else launches2, 1)
     pts_fp64 = args.steps * n_inst * L / max(launches2 if headline_split else launches, 1)
     split_bytes = ((241.858816e6 + 20.879104e6) if args.no_edge_store else
-                   (237.687808e6 + 23.139072e6))
+                   (237.686784e6 + 22.566656e6))
     roof_split["traffic"] = split_bytes / (8 * L_FULL) * pts_split
     roof_fp64["traffic"] = 53.188352e6 / L_FULL * pts_fp64
 
