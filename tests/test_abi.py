@@ -28,3 +28,29 @@ def test_status_strings():
     lib = _capi.load(build.build())
     assert lib.qew_status_string(0) == b"ok"
     assert b"even" in lib.qew_status_string(_capi.QEW_ERR_ODD_LENGTH)
+
+
+def test_header_constants_match_python_mirror():
+    """Every enum constant and numeric #define of the public headers has the
+    same value in the Python mirror, and the mirror defines each one the
+    bindings use."""
+    import re
+
+    import qew_gb300 as Q
+    txt = "".join(open(h).read() for h in _capi.HEADERS)
+    consts = {}
+    for body in re.findall(r"\benum\s*\{([^}]*)\}", txt):
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        for name, val in re.findall(r"\b(QEW_[A-Z0-9_]+)\s*=\s*(-?\d+)", body):
+            consts[name] = int(val)
+    for name, val in re.findall(r"^#define\s+(QEW_[A-Z0-9_]+)\s+(-?\d+)\s*$", txt, re.M):
+        consts[name] = int(val)
+    assert len(consts) >= 28
+    mirrored = {k: v for k, v in consts.items() if hasattr(_capi, k)}
+    for name, val in mirrored.items():
+        assert getattr(_capi, name) == val, name
+    need = [k for k in consts if k.startswith(("QEW_ERR_", "QEW_STORE_", "QEW_PREC_", "QEW_FIELD_",
+                                               "QEW_REQ_", "QEW_RK_", "QEW_LBFGS_"))]
+    assert set(need) <= set(mirrored), sorted(set(need) - set(mirrored))
+    assert int(Q.Model.Linear) == consts["QEW_MODEL_LINEAR"]
+    assert int(Q.Model.Arclength) == consts["QEW_MODEL_ARCLENGTH"]
