@@ -246,7 +246,12 @@ qew_status qew_gradient_host_batch(qew_ctx *ctx, const qew_field *field,
  * counterpart). Heights are carried in field y-cells as an integer cell plus
  * an FP32 fraction, h = (cell + frac) * dy. qew_split_heights / join convert
  * from / to FP64 heights; qew_gradient_split is gradient() (qew_model.h:149-201)
- * on split heights with FP32 output. Needs a field stored with QEW_STORE_FP32. */
+ * on split heights with FP32 output. Needs a field stored with QEW_STORE_FP32.
+ * When the field also holds QEW_STORE_FP32_EDGE and the line has one point
+ * per field column (n == nx, physical_size == Lx), each edge reads the
+ * x-filtered store: 4 values instead of 16 taps, one persistent launch. The
+ * result stays within the same error bound; it is not bitwise equal to the
+ * 16-tap form, whose x sum runs in a different order. */
 qew_status qew_split_heights(qew_ctx *ctx, const qew_field *field,
                              const double *d_h, int n, int32_t *d_cell,
                              float *d_frac);
