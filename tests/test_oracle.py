@@ -230,3 +230,34 @@ def test_oracle_fire_reference_cases(O):
     r = O.fire_minimize(h, O.params(64.0, 1.0, 0.0, 0), O.HarmonicWell(2.0, 0.5),
                         O.fire_params(0.1, ftol=1e-12, max_iter=3))
     assert not r.converged and r.iterations == 3
+
+
+def test_x_filtered_store_identity(O):
+    """The x-filtered store's algebra: on a line with one point per field
+    column, the midpoint of edge e sits at x = (e + 1/2) dx, where the cubic
+    B-spline x weights are 1/48, 23/48, 23/48, 1/48. The per-column x sums
+    E[e, j] = sum_a w_a c[e - 1 + a, j], weighted along y, reproduce the
+    oracle's 16-tap value and dV/dy there (to rounding, the sum's order
+    aside)."""
+    nx, ny, Lx, Ly = 64, 16, 64.0, 8.0
+    rng = np.random.default_rng(11)
+    fld = rng.standard_normal((nx, ny))
+    of = O.BSplineField(fld, Lx, Ly)
+    c = of.coef                                  # [nx][ny], y fastest
+    w = np.array([1.0, 23.0, 23.0, 1.0]) / 48.0
+    E = sum(w[a] * np.roll(c, 1 - a, axis=0) for a in range(4))   # E[e] uses c[e-1+a]
+    dx, dy = Lx / nx, Ly / ny
+    e = np.repeat(np.arange(nx - 1), 5)          # every edge but the wrap edge
+    y = rng.uniform(-2 * Ly, 3 * Ly, e.size)     # rows wrap on both sides
+    gy = y / dy
+    iy = np.floor(gy).astype(int)
+    t = gy - iy
+    wy = np.stack([(1 - t) ** 3, 3 * t ** 3 - 6 * t ** 2 + 4, -3 * t ** 3 + 3 * t ** 2 + 3 * t + 1,
+                   t ** 3]) / 6.0
+    dwy = np.stack([-0.5 * (1 - t) ** 2, 1.5 * t ** 2 - 2 * t, -1.5 * t ** 2 + t + 0.5, 0.5 * t ** 2])
+    rows = [(iy - 1 + b) % ny for b in range(4)]
+    v = sum(wy[b] * E[e, rows[b]] for b in range(4))
+    dvdy = sum(dwy[b] * E[e, rows[b]] for b in range(4)) / dy
+    vo, _, dvdyo = O.sample(of, (e + 0.5) * dx, y)
+    assert np.max(np.abs(v - vo)) <= 1e-13 * np.max(np.abs(vo))
+    assert np.max(np.abs(dvdy - dvdyo)) <= 1e-13 * np.max(np.abs(dvdyo))
