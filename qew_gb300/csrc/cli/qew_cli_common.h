@@ -8,6 +8,7 @@
 #include <exception>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "qew_cli.h"
 #include "qew_gpu.h"
@@ -48,6 +49,19 @@ class Gpu {
         check(qew_field_create_seeded(ctx, nx, ny, Lx, Ly, amplitude, xi, xi, seed, store, &field),
               "field");
     }
+    // FilteredNoise(field, nx, ny, Lx, Ly) (filtered_noise.h:186-189): a given
+    // real-space field in the host layout [nx][ny].
+    void host_field(const std::vector<double> &f, int nx, int ny, double Lx, double Ly, int store) {
+        check(qew_field_create_from_host(ctx, f.data(), nx, ny, Lx, Ly, store, &field), "field");
+    }
+    // The executables' field: the file's when one was given, else the seeded one.
+    void field_for(const std::vector<double> &file_field, int nx, int ny, double Lx, double Ly,
+                   double amplitude, double xi, uint64_t seed, int store) {
+        if (!file_field.empty())
+            host_field(file_field, nx, ny, Lx, Ly, store);
+        else
+            seeded_field(nx, ny, Lx, Ly, amplitude, xi, seed, store);
+    }
     void check(qew_status s, const char *what) {
         if (s != QEW_OK)
             throw GpuError(std::string(what) + ": " + qew_status_string(s) +
@@ -56,6 +70,37 @@ class Gpu {
     qew_ctx *ctx = nullptr;
     qew_field *field = nullptr;
 };
+
+// --rows R: R field rows at unit grid spacing (ny = R, Ly = R), the layout
+// of the benchmark configurations. Not together with --ny or --Ly. Call it
+// right after reading ny and Ly, before anything derived from them.
+inline void apply_rows(Options &a, int &ny, double &Ly) {
+    if (!a.has("rows")) return;
+    if (a.has("ny") || a.has("Ly"))
+        throw std::runtime_error("--rows sets --ny and --Ly; give either --rows or those");
+    const int r = a.integer("rows", 0);
+    if (r < 1) throw std::runtime_error("--rows must be positive");
+    ny = r;
+    Ly = (double)r;
+}
+
+// --field_file PATH: the real-space field as a float64 .npy array of shape
+// (nx, ny), used in place of the seeded one (the reference's
+// FilteredNoise(field, nx, ny, Lx, Ly)). Its shape sets nx and ny; --nx and
+// --ny must match it when given. Returns an empty vector without the option.
+inline std::vector<double> field_from_file(Options &a, int &nx, int &ny) {
+    const std::string path = a.text("field_file", "");
+    if (path.empty()) return {};
+    int rows = 0, cols = 0;
+    std::vector<double> f = read_npy_f64_2d(path, rows, cols);
+    if ((a.has("nx") && rows != nx) || ((a.has("ny") || a.has("rows")) && cols != ny))
+        throw std::runtime_error("--field_file '" + path + "' has shape (" + std::to_string(rows) +
+                                 ", " + std::to_string(cols) + "), not the given --nx/--ny (" +
+                                 std::to_string(nx) + ", " + std::to_string(ny) + ")");
+    nx = rows;
+    ny = cols;
+    return f;
+}
 
 // ell, acf, q, psd of one host profile (qew_line_statistics_host).
 inline LineStats line_stats(Gpu &gpu, const std::vector<double> &h, double L) {

@@ -3,7 +3,8 @@
 // same options, defaults (RK knobs derived from Ly/ny), console lines and
 // output keys, on the GPU. Added options: --bisect_rtol (bisect f_c after
 // the ramp; adds the key f_c), --precision fp64|fp32split, --analysis 1 (ell,
-// acf, q, psd beside each blocked profile), --device.
+// acf, q, psd beside each blocked profile), --field_file (a given field),
+// --rows (unit-spacing rows), --device.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -31,6 +32,8 @@ const char *kUsage =
     "  --bisect_rtol     bisect f_c to this relative width after the ramp (default 0: off)\n"
     "  --precision       fp64|fp32split         (default fp64)\n"
     "  --analysis        1: add ell, acf, q, psd beside each blocked profile (default 0)\n"
+    "  --field_file      float64 .npy field, shape (nx, ny), instead of the seeded one\n"
+    "  --rows            R rows at unit spacing: --ny R --Ly R\n"
     "  --device          CUDA device            (default 0)\n";
 
 struct Collect {
@@ -61,6 +64,8 @@ int run(int argc, char **argv) {
     cfg.Ly = a.real("Ly", 1.0);
     cfg.nx = a.integer("nx", 1024);
     cfg.ny = a.integer("ny", 256);
+    cli::apply_rows(a, cfg.ny, cfg.Ly);
+    const std::vector<double> file_field = cli::field_from_file(a, cfg.nx, cfg.ny);
     cfg.f_step = a.real("f_step", 1.0);
     cfg.f_max = a.real("f_max", 40.0);
     cfg.rp.dstep = a.real("dstep", 0.5 * (cfg.Ly / cfg.ny));
@@ -80,7 +85,7 @@ int run(int argc, char **argv) {
 
     cli::Gpu gpu(device);
     const int store = QEW_STORE_FP64 | (cfg.precision == QEW_PREC_FP32_SPLIT ? QEW_STORE_FP32 : 0);
-    gpu.seeded_field(cfg.nx, cfg.ny, cfg.Lx, cfg.Ly, cfg.amplitude, cfg.xi, seed, store);
+    gpu.field_for(file_field, cfg.nx, cfg.ny, cfg.Lx, cfg.Ly, cfg.amplitude, cfg.xi, seed, store);
     Collect col;
     qew_depinning_result res{};
     gpu.check(qew_depinning_ramp(gpu.ctx, gpu.field, &cfg, &Collect::on, &col, &res),

@@ -2,7 +2,8 @@
 // reference's dynamic run (executables/qew_dynamic/main.cpp) with the same
 // options, defaults, console lines and output keys, on the GPU. Added
 // options: --dt (explicit timestep), --precision fp64|fp32split, --analysis 1
-// (ell, acf, q, psd beside each snapshot), --device.
+// (ell, acf, q, psd beside each snapshot), --field_file (a given field),
+// --rows (unit-spacing rows), --device.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -31,6 +32,8 @@ const char *kUsage =
     "  --dt              timestep               (default: from xi and the thermal lengths)\n"
     "  --precision       fp64|fp32split         (default fp64)\n"
     "  --analysis        1: add ell, acf, q, psd beside each snapshot (default 0)\n"
+    "  --field_file      float64 .npy field, shape (nx, ny), instead of the seeded one\n"
+    "  --rows            R rows at unit spacing: --ny R --Ly R\n"
     "  --device          CUDA device            (default 0)\n";
 
 struct Collect {
@@ -58,6 +61,8 @@ int run(int argc, char **argv) {
     cfg.Ly = a.real("Ly", 1.0);
     cfg.nx = a.integer("nx", 2048);
     cfg.ny = a.integer("ny", 1024);
+    cli::apply_rows(a, cfg.ny, cfg.Ly);
+    const std::vector<double> file_field = cli::field_from_file(a, cfg.nx, cfg.ny);
     cfg.seed = a.u64("seed", 1);
     cfg.tau = a.real("tau", 1.0);
     cfg.tl_start = a.real("tl_start", 0.01);
@@ -73,7 +78,8 @@ int run(int argc, char **argv) {
 
     cli::Gpu gpu(device);
     const int store = QEW_STORE_FP64 | (cfg.precision == QEW_PREC_FP32_SPLIT ? QEW_STORE_FP32 : 0);
-    gpu.seeded_field(cfg.nx, cfg.ny, cfg.Lx, cfg.Ly, cfg.amplitude, cfg.xi, cfg.seed, store);
+    gpu.field_for(file_field, cfg.nx, cfg.ny, cfg.Lx, cfg.Ly, cfg.amplitude, cfg.xi, cfg.seed,
+                  store);
     Collect col;
     qew_dynamic_result res{};
     gpu.check(qew_dynamic_anneal(gpu.ctx, gpu.field, &cfg, &Collect::on, &col, &res),

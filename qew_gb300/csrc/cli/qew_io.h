@@ -1,4 +1,5 @@
-// qew_io.h -- output of the three simulation executables.
+// qew_io.h -- output of the three simulation executables (and the .npy
+// reader of their --field_file input).
 //
 // The dataset KEYS are the reference's contract with its analysis scripts
 // (qew_io.h:22-63, qew_format.h:13-17, pinned by test_executables.cpp:50-56
@@ -11,6 +12,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -24,6 +26,88 @@
 #endif
 
 namespace qew {
+
+// A float64 2-D array from a .npy file (format versions 1-3, little-endian
+// '<f8', C order), e.g. the real-space field of --field_file: shape (nx, ny),
+// x slow and y fast, the reference's host layout (filtered_noise.h:208).
+// Anything else (another dtype, Fortran order, another rank, a short file)
+// is an error.
+inline std::vector<double> read_npy_f64_2d(const std::string &path, int &rows, int &cols) {
+    const uint16_t one = 1;
+    unsigned char lsb;
+    std::memcpy(&lsb, &one, 1);
+    if (lsb != 1) throw std::runtime_error("reading .npy needs a little-endian host");
+    std::unique_ptr<std::FILE, int (*)(std::FILE *)> f(std::fopen(path.c_str(), "rb"), &std::fclose);
+    if (!f) throw std::runtime_error("cannot open '" + path + "'");
+    const std::string what = "'" + path + "': ";
+    unsigned char pre[8];
+    if (std::fread(pre, 1, 8, f.get()) != 8 || std::memcmp(pre, "\x93NUMPY", 6) != 0)
+        throw std::runtime_error(what + "not a .npy file");
+    size_t hlen = 0;
+    if (pre[6] == 1) {
+        unsigned char b[2];
+        if (std::fread(b, 1, 2, f.get()) != 2) throw std::runtime_error(what + "short header");
+        hlen = (size_t)b[0] | (size_t)b[1] << 8;
+    } else if (pre[6] == 2 || pre[6] == 3) {
+        unsigned char b[4];
+        if (std::fread(b, 1, 4, f.get()) != 4) throw std::runtime_error(what + "short header");
+        hlen = (size_t)b[0] | (size_t)b[1] << 8 | (size_t)b[2] << 16 | (size_t)b[3] << 24;
+    } else {
+        throw std::runtime_error(what + "unsupported .npy version");
+    }
+    if (hlen == 0 || hlen > (1u << 20)) throw std::runtime_error(what + "bad header length");
+    std::string hdr(hlen, '\0');
+    if (std::fread(&hdr[0], 1, hlen, f.get()) != hlen) throw std::runtime_error(what + "short header");
+    auto value_of = [&](const char *key) {  // text after 'key': up to the next ',' or '}' at depth 0
+        const std::string k = std::string("'") + key + "'";
+        size_t at = hdr.find(k);
+        if (at == std::string::npos) throw std::runtime_error(what + "header lacks " + k);
+        at = hdr.find(':', at + k.size());
+        if (at == std::string::npos) throw std::runtime_error(what + "bad header");
+        size_t end = at + 1;
+        int depth = 0;
+        for (; end < hdr.size(); ++end) {
+            const char c = hdr[end];
+            if (c == '(') ++depth;
+            if (c == ')') --depth;
+            if (depth == 0 && (c == ',' || c == '}')) break;
+        }
+        std::string v = hdr.substr(at + 1, end - at - 1);
+        const size_t b = v.find_first_not_of(" "), e = v.find_last_not_of(" ");
+        return b == std::string::npos ? std::string() : v.substr(b, e - b + 1);
+    };
+    if (value_of("descr") != "'<f8'") throw std::runtime_error(what + "dtype must be float64 ('<f8')");
+    if (value_of("fortran_order") != "False") throw std::runtime_error(what + "must be C order");
+    const std::string shape = value_of("shape");
+    std::vector<long long> d;  // the tuple's items: "(a, b)", spaces and a trailing comma allowed
+    if (shape.size() < 2 || shape.front() != '(' || shape.back() != ')')
+        throw std::runtime_error(what + "bad shape " + shape);
+    size_t pos = 1;
+    while (pos < shape.size() - 1) {
+        size_t comma = shape.find(',', pos);
+        if (comma == std::string::npos || comma > shape.size() - 1) comma = shape.size() - 1;
+        std::string item = shape.substr(pos, comma - pos);
+        item.erase(0, item.find_first_not_of(' '));
+        item.erase(item.find_last_not_of(' ') + 1);
+        if (!item.empty()) {
+            char *end = nullptr;
+            const long long v = std::strtoll(item.c_str(), &end, 10);
+            if (*end != '\0') throw std::runtime_error(what + "bad shape " + shape);
+            d.push_back(v);
+        }
+        pos = comma + 1;
+    }
+    if (d.size() != 2) throw std::runtime_error(what + "must be a 2-D array, shape " + shape);
+    if (d[0] < 1 || d[1] < 1 || d[0] > INT32_MAX || d[1] > INT32_MAX)
+        throw std::runtime_error(what + "bad shape " + shape);
+    const size_t count = (size_t)d[0] * (size_t)d[1];
+    std::vector<double> out(count);
+    if (std::fread(out.data(), sizeof(double), count, f.get()) != count)
+        throw std::runtime_error(what + "fewer values than its shape");
+    rows = (int)d[0];
+    cols = (int)d[1];
+    return out;
+}
 
 // printf into a std::string (qew_format.h:13-17).
 inline std::string fmt(const char *spec, double v) {

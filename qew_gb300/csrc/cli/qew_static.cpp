@@ -3,7 +3,7 @@
 // with the same options, defaults, console lines and output keys, on the GPU.
 // Added options: --lbfgs_m (history size), --analysis 1 (write ell, acf, q,
 // psd beside each profile, as the reference's post-processing does),
-// --device.
+// --field_file (a given field), --rows (unit-spacing rows), --device.
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -29,6 +29,8 @@ const char *kUsage =
     "  --output          output file            (default static_<model>.npz, .h5 with HDF5)\n"
     "  --lbfgs_m         L-BFGS history size    (default 8)\n"
     "  --analysis        1: add ell, acf, q, psd beside each profile (default 0)\n"
+    "  --field_file      float64 .npy field, shape (nx, ny), instead of the seeded one\n"
+    "  --rows            R rows at unit spacing: --ny R --Ly R\n"
     "  --device          CUDA device            (default 0)\n";
 
 int run(int argc, char **argv) {
@@ -47,6 +49,8 @@ int run(int argc, char **argv) {
     cfg.Ly = a.real("Ly", 1.0);
     cfg.nx = a.integer("nx", 4096);
     cfg.ny = a.integer("ny", 512);
+    cli::apply_rows(a, cfg.ny, cfg.Ly);
+    const std::vector<double> file_field = cli::field_from_file(a, cfg.nx, cfg.ny);
     cfg.driving_force = a.real("driving_force", 0.0);
     const std::vector<double> ratios =
         a.real_list("pinning_lengths", {0.01, 0.1, 1.0, 10.0, 100.0});
@@ -63,7 +67,8 @@ int run(int argc, char **argv) {
     std::unique_ptr<Sink> sink = open_sink(fname);
 
     cli::Gpu gpu(device);
-    gpu.seeded_field(cfg.nx, cfg.ny, cfg.Lx, cfg.Ly, cfg.amplitude, cfg.xi, seed, QEW_STORE_FP64);
+    gpu.field_for(file_field, cfg.nx, cfg.ny, cfg.Lx, cfg.Ly, cfg.amplitude, cfg.xi, seed,
+                  QEW_STORE_FP64);
     std::vector<qew_static_profile> prof(ratios.size());
     std::vector<double> h(ratios.size() * (size_t)cfg.nx);
     gpu.check(qew_static_sweep(gpu.ctx, gpu.field, &cfg, prof.data(), h.data()), "static_sweep");

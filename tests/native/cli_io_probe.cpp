@@ -4,7 +4,9 @@
 //                    (tests/test_cli.cpp) and prints what it got;
 //   QEW_PROBE=fmt    prints the key formatter's strings (test_executables.cpp:50-56);
 //   QEW_PROBE=write  writes the three fixtures of test_executables.cpp:199-289
-//                    as .npz files into the directory given as argv[1].
+//                    as .npz files into the directory given as argv[1];
+//   QEW_PROBE=npy    reads the float64 .npy array argv[1] (the --field_file
+//                    reader) and prints its shape and a few values.
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -78,5 +80,20 @@ int main(int argc, char **argv) {
         return 0;
     }
     if (m == "write") return argc > 1 ? write(argv[1]) : 1;
+    if (m == "npy") {
+        if (argc < 2) return 1;
+        try {
+            int rows = 0, cols = 0;
+            const std::vector<double> v = read_npy_f64_2d(argv[1], rows, cols);
+            double sum = 0.0;
+            for (double x : v) sum += x;
+            std::printf("rows=%d\ncols=%d\nfirst=%.17g\nlast=%.17g\nsum=%.17g\n", rows, cols,
+                        v.front(), v.back(), sum);
+            return 0;
+        } catch (const std::exception &e) {
+            std::printf("error=%s\n", e.what());
+            return 2;
+        }
+    }
     return parse(argc, argv);
 }

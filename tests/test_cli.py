@@ -149,3 +149,58 @@ def test_cpp_face_compiles_and_links(tmp_path):
     """include/qew_gpu.hpp: the reference's signatures over the C ABI build
     against the library (it runs in tests/test_gpu_runs.py)."""
     assert os.path.exists(build_hpp_probe(tmp_path))
+
+
+def _npy(probe, path):
+    r = subprocess.run([probe, str(path)], capture_output=True, text=True,
+                       env=dict(os.environ, QEW_PROBE="npy"))
+    return r.returncode, dict(ln.split("=", 1) for ln in r.stdout.splitlines() if "=" in ln)
+
+
+def test_field_file_reader(probe, tmp_path):
+    """The --field_file reader: float64 C-order 2-D .npy (header versions 1
+    and 2), shape and values as numpy wrote them; anything else rejected."""
+    a = np.random.default_rng(0).standard_normal((7, 5))
+    np.save(tmp_path / "f.npy", a)
+    rc, v = _npy(probe, tmp_path / "f.npy")
+    assert rc == 0 and (v["rows"], v["cols"]) == ("7", "5")
+    assert float(v["first"]) == a[0, 0] and float(v["last"]) == a[-1, -1]
+    assert abs(float(v["sum"]) - a.sum()) < 1e-12
+    with open(tmp_path / "v2.npy", "wb") as fh:
+        np.lib.format.write_array(fh, a, version=(2, 0))
+    rc, v = _npy(probe, tmp_path / "v2.npy")
+    assert rc == 0 and (v["rows"], v["cols"]) == ("7", "5")
+    bad = {
+        "f32.npy": a.astype(np.float32), "fortran.npy": np.asfortranarray(a),
+        "one_d.npy": a.ravel(), "three_d.npy": a.reshape(7, 5, 1), "big_endian.npy": a.astype(">f8"),
+    }
+    for name, arr in bad.items():
+        np.save(tmp_path / name, arr)
+        rc, v = _npy(probe, tmp_path / name)
+        assert rc == 2 and "error" in v, name
+    raw = (tmp_path / "f.npy").read_bytes()
+    (tmp_path / "short.npy").write_bytes(raw[:-8])
+    (tmp_path / "text.npy").write_bytes(b"not an array")
+    for name in ("short.npy", "text.npy", "missing.npy"):
+        rc, v = _npy(probe, tmp_path / name)
+        assert rc == 2 and "error" in v, name
+
+
+@pytest.mark.parametrize("name", ["qew_static", "qew_dynamic", "qew_depinning"])
+def test_executables_field_file_and_rows_errors(name, tmp_path):
+    """--field_file / --rows mistakes end with exit 2, the message and the
+    usage, before any GPU work."""
+    exe = _exe(name)
+    np.save(tmp_path / "f.npy", np.zeros((4, 3)))
+    cases = [
+        (["--rows", "16", "--ny", "8"], "--rows"),
+        (["--rows", "16", "--Ly", "2"], "--rows"),
+        (["--rows", "0"], "--rows"),
+        (["--field_file", str(tmp_path / "missing.npy")], "cannot open"),
+        (["--field_file", str(tmp_path / "f.npy"), "--nx", "5"], "has shape (4, 3)"),
+        (["--field_file", str(tmp_path / "f.npy"), "--rows", "8"], "has shape (4, 3)"),
+    ]
+    for args, msg in cases:
+        r = subprocess.run([exe, *args], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 2, (args, r.stderr)
+        assert msg in r.stderr and "--field_file" in r.stderr, (args, r.stderr)
