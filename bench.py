@@ -254,7 +254,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": headline_config(L, NY_FULL, N_INST, args.precision, 1),
+            "config": headline_config(L, NY_FULL, N_INST, args.precision, ws),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": O.omp_max_threads(),
                              "kind": "port",
                              "sample": "per step one of the workload's 2^20-point lines (FP64, the "
