@@ -732,10 +732,14 @@ def run_ours(args):
             Q.gradient_host_batch(hh, p, noise, gh, precision=prec)
         torch.cuda.synchronize()
         e2e_steps = max(3, args.steps // 2)
+        if ws > 1:
+            torch.distributed.barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             Q.gradient_host_batch(hh, p, noise, gh, precision=prec)
         dt = time.perf_counter() - t0
+        if ws > 1:  # the slowest replica's time, as for the device-timed value
+            dt = max_over_ranks(torch, dt * 1e3, "cuda") * 1e-3
         e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
                "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
                "call": "qew_gradient_host_batch: the step's 8 lines as FP64 pinned host heights "
