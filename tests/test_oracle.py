@@ -261,3 +261,59 @@ def test_x_filtered_store_identity(O):
     vo, _, dvdyo = O.sample(of, (e + 0.5) * dx, y)
     assert np.max(np.abs(v - vo)) <= 1e-13 * np.max(np.abs(vo))
     assert np.max(np.abs(dvdy - dvdyo)) <= 1e-13 * np.max(np.abs(dvdyo))
+
+
+def test_oracle_dynamics_known_answers(O):
+    """The oracle's Langevin step against the reference's dynamics known
+    answers (test_dynamics.cpp:40-161), harmonic trough k = 4, linear model,
+    dx = 1; the oracle takes the N(0,1) increments from the caller."""
+    rng = np.random.default_rng(0)
+    # T = 0 is gradient descent: the energy never rises and relaxes to 0 (44-65)
+    n = 64
+    p, well = O.params(float(n), 1.0, 0.0, 0), O.HarmonicWell(4.0, 0.0)
+    h = rng.uniform(-0.5, 0.5, n)
+    zero = np.zeros(n)
+    e_prev = O.objective(h, p, well)
+    for _ in range(2000):
+        O.langevin_step(h, p, well, 0.05, 0.0, zero)
+        e = O.objective(h, p, well)
+        assert e <= e_prev + 1e-12
+        e_prev = e
+    assert e_prev < 1e-6
+    # a driving force shifts the equilibrium to y0 + f/k (106-130)
+    n, k, y0, f = 32, 4.0, 0.2, 0.6
+    p, well = O.params(float(n), 1.0, f, 0), O.HarmonicWell(k, y0)
+    h = np.zeros(n)
+    for _ in range(5000):
+        O.langevin_step(h, p, well, 0.05, 0.0, np.zeros(n))
+    assert np.max(np.abs(h - (y0 + f / k))) < 1e-6
+    # diff = 0 ignores the increments entirely (137-161)
+    n = 48
+    p, well = O.params(float(n), 1.0, 0.3, 0), O.HarmonicWell(4.0, 0.1)
+    h1 = rng.uniform(-0.5, 0.5, n)
+    h2 = h1.copy()
+    for _ in range(50):
+        O.langevin_step(h1, p, well, 0.05, 0.0, rng.standard_normal(n))
+        O.langevin_step(h2, p, well, 0.05, 0.0, rng.standard_normal(n))
+    assert np.array_equal(h1, h2)
+
+
+def test_oracle_equipartition(O):
+    """<E> = (N/2) kT with kT = diff^2 / (2 drift) (test_dynamics.cpp:70-99),
+    within 10 %, on a shorter run than the reference's."""
+    n, drift, kT = 16, 0.02, 0.05
+    diff = np.sqrt(2 * drift * kT)
+    p, well = O.params(float(n), 1.0, 0.0, 0), O.HarmonicWell(4.0, 0.0)
+    rng = np.random.default_rng(2024)
+    h = np.zeros(n)
+    n_equil, n_sample, block = 5000, 60000, 5000
+    for _ in range(n_equil // block):
+        for xi in rng.standard_normal((block, n)):
+            O.langevin_step(h, p, well, drift, diff, xi)
+    total = 0.0
+    for _ in range(n_sample // block):
+        for xi in rng.standard_normal((block, n)):
+            O.langevin_step(h, p, well, drift, diff, xi)
+            total += O.objective(h, p, well)
+    mean_e, expected = total / n_sample, 0.5 * n * kT
+    assert abs(mean_e - expected) < 0.1 * expected, mean_e
