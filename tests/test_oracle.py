@@ -317,3 +317,19 @@ def test_oracle_equipartition(O):
             total += O.objective(h, p, well)
     mean_e, expected = total / n_sample, 0.5 * n * kT
     assert abs(mean_e - expected) < 0.1 * expected, mean_e
+
+
+def test_oracle_seeded_field_amplitude_and_band_limit(O):
+    """The seeded generator's known answer (test_filtered_noise.cpp:68-111): the
+    field's population std is the amplitude, and its Fourier modes outside the
+    correlation ellipse (fx xi_x)^2 + (fy xi_y)^2 > 1 vanish."""
+    nx, ny, Lx, Ly, amp, xi_x, xi_y = 128, 96, 4.0, 1.0, 2.0, 0.2, 0.1
+    f = O.seeded_field(nx, ny, Lx, Ly, amp, xi_x, xi_y, 42)
+    assert f.shape == (nx, ny)
+    assert abs(f.std() - amp) < 1e-10
+    mag = np.abs(np.fft.fft2(f))
+    fx = np.fft.fftfreq(nx, d=Lx / nx)[:, None]
+    fy = np.fft.fftfreq(ny, d=Ly / ny)[None, :]
+    masked = (fx * xi_x) ** 2 + (fy * xi_y) ** 2 > 1.0
+    assert masked.any() and (~masked).sum() > 1
+    assert mag[masked].max() < 1e-8 * mag.max()
