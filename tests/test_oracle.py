@@ -333,3 +333,53 @@ def test_oracle_seeded_field_amplitude_and_band_limit(O):
     masked = (fx * xi_x) ** 2 + (fy * xi_y) ** 2 > 1.0
     assert masked.any() and (~masked).sum() > 1
     assert mag[masked].max() < 1e-8 * mag.max()
+
+
+def _seeded_bspline(O, nx, ny, Lx, Ly, amp, xi, seed):
+    """FilteredNoise(nx, ny, Lx, Ly, amp, xi, xi, seed) of the reference."""
+    return O.BSplineField(O.seeded_field(nx, ny, Lx, Ly, amp, xi, xi, seed), Lx, Ly)
+
+
+def _max_site_velocity(O, h, p, f):
+    return float(np.max(-O.gradient(h, p, f)))
+
+
+def test_rk_blocked_config_forward_and_arrested(O):
+    """test_rosso_krauth.cpp:143-186 (linear) and 250-291 (arclength): the
+    blocked line lies forward of the flat start and no site has a positive
+    velocity."""
+    for (amp, seed, lt, force, model) in ((0.5, 7, 1.0, 0.0, 0), (0.6, 29, 1.2, 0.1, 1)):
+        nx, ny, Lx, Ly = 64, 64, 3.2, 1.0
+        f = _seeded_bspline(O, nx, ny, Lx, Ly, amp, 0.2, seed)
+        p = O.params(Lx, lt, force, model)
+        h = np.full(nx, 0.5 * Ly)
+        h0 = h.copy()
+        r = O.rk_block(h, p, f, O.rk_params(0.5 * Ly / ny, Ly, 1e-11, 1e-9, 3 * Ly, 200000))
+        assert r.blocked
+        assert np.all(h >= h0 - 1e-12)
+        assert _max_site_velocity(O, h, p, f) < 1e-6
+
+
+def test_rk_deterministic(O):
+    """test_rosso_krauth.cpp:189-216: the same force and start give the same
+    blocked line, bit for bit (arclength, f = 0.3)."""
+    nx, ny, Lx, Ly = 48, 48, 2.4, 1.0
+    f = _seeded_bspline(O, nx, ny, Lx, Ly, 0.5, 0.2, 9)
+    p = O.params(Lx, 1.5, 0.3, 1)
+    rp = O.rk_params(0.5 * Ly / ny, Ly, 1e-11, 1e-9, 5 * Ly, 200000)
+    a, b = np.full(nx, 0.5 * Ly), np.full(nx, 0.5 * Ly)
+    O.rk_block(a, p, f, rp)
+    O.rk_block(b, p, f, rp)
+    assert np.array_equal(a, b)
+
+
+def test_rk_runaway_flag(O):
+    """test_rosso_krauth.cpp:223-248: at twice the washboard's f_c the sweep
+    reports runaway (not merely not blocked) past the runaway distance."""
+    n, A, k = 16, 0.1, 2 * PI
+    lam = 2 * PI / k
+    p = O.params(float(n), 1.0, 2.0 * A * k, 0)
+    rp = O.rk_params(lam / 200, lam, 1e-12, 1e-11, 3 * lam, 100000)
+    r = O.rk_block(np.zeros(n), p, O.SinusoidNoise(A, k), rp)
+    assert r.runaway and not r.blocked
+    assert r.mean_h > rp.runaway
