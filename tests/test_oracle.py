@@ -383,3 +383,47 @@ def test_rk_runaway_flag(O):
     r = O.rk_block(np.zeros(n), p, O.SinusoidNoise(A, k), rp)
     assert r.runaway and not r.blocked
     assert r.mean_h > rp.runaway
+
+
+def test_lbfgs_restart_fast_fire_and_preconditioner(O):
+    """test_lbfgs.cpp:200-304 on the oracle: a clamped line search (max_ls = 3)
+    takes the restart branch where the normal budget converges without one; a
+    quadratic converges in < 200 iterations; L-BFGS and FIRE reach the same
+    minimum to 1e-5; the preconditioner converges a stiff line (Gamma = 50,
+    dx = 0.01) in < 300 iterations, fewer than without it."""
+    import math
+    nx, ny, Lx, Ly = 64, 64, 3.2, 1.0
+    f = _seeded_bspline(O, nx, ny, Lx, Ly, 2.0, 0.15, 3)
+    p = O.params(Lx, 0.5, 0.0, 0)
+    h = np.full(nx, 0.5 * Ly)
+    r = O.lbfgs_minimize(h, p, f, O.lbfgs_default_params(ftol=1e-6, max_iter=50000, max_ls=3))
+    assert r.n_ls_restarts > 0
+    h = np.full(nx, 0.5 * Ly)
+    r = O.lbfgs_minimize(h, p, f, O.lbfgs_default_params(ftol=1e-6, max_iter=50000, max_ls=30))
+    assert r.converged and r.n_ls_restarts == 0
+
+    n = 128
+    h = np.zeros(n)
+    r = O.lbfgs_minimize(h, O.params(float(n), 1.0, 0.0, 0), O.HarmonicWell(1.0, 0.3),
+                         O.lbfgs_default_params(ftol=1e-8))
+    assert r.converged and r.iterations < 200
+
+    n = 96
+    p = O.params(float(n), 1.0, 0.0, 0)
+    init = np.random.default_rng(3).uniform(0.0, 1.0, n)
+    a, b = init.copy(), init.copy()
+    O.lbfgs_minimize(a, p, O.HarmonicWell(1.5, 0.4), O.lbfgs_default_params(ftol=1e-9))
+    O.fire_minimize(b, p, O.HarmonicWell(1.5, 0.4), O.fire_params(0.1 * math.sqrt(1.0), ftol=1e-9))
+    assert np.max(np.abs(a - b)) < 1e-5
+
+    nx, ny, Lx, Ly = 256, 64, 2.56, 1.0
+    f = _seeded_bspline(O, nx, ny, Lx, Ly, 0.3, 0.2, 5)
+    p = O.params(Lx, 50.0, 0.0, 0)
+    h = np.full(nx, 0.5 * Ly)
+    r = O.lbfgs_minimize(h, p, f, O.lbfgs_default_params(ftol=1e-6, max_iter=5000,
+                                                         precondition=1))
+    assert r.converged and r.iterations < 300
+    h = np.full(nx, 0.5 * Ly)
+    r2 = O.lbfgs_minimize(h, p, f, O.lbfgs_default_params(ftol=1e-6, max_iter=5000,
+                                                          precondition=0))
+    assert r.iterations < r2.iterations
