@@ -427,3 +427,24 @@ def test_lbfgs_restart_fast_fire_and_preconditioner(O):
     r2 = O.lbfgs_minimize(h, p, f, O.lbfgs_default_params(ftol=1e-6, max_iter=5000,
                                                           precondition=0))
     assert r.iterations < r2.iterations
+
+
+def test_oracle_fire_lowers_energy_and_is_deterministic(O):
+    """test_fire.cpp:108-160 on the oracle: FIRE does not raise the energy
+    (arclength, random start) and identical inputs give identical results."""
+    import math
+    n = 96
+    p = O.params(float(n), 1.0, 0.0, 1)
+    well = O.HarmonicWell(1.5, 0.6)
+    h = np.random.default_rng(1).uniform(0.0, 1.0, n)
+    e0 = O.objective(h, p, well)
+    O.fire_minimize(h, p, well, O.fire_params(0.1 * math.sqrt(1.0), ftol=1e-9))
+    assert O.objective(h, p, well) <= e0 + 1e-12
+    n = 64
+    p = O.params(float(n), 1.0, 0.0, 0)
+    well = O.HarmonicWell(1.0, 0.5)
+    init = 0.3 * np.sin(2 * np.pi * np.arange(n) / n)
+    a, b = init.copy(), init.copy()
+    fp = O.fire_params(0.1, ftol=1e-10)
+    r1, r2 = O.fire_minimize(a, p, well, fp), O.fire_minimize(b, p, well, fp)
+    assert r1.iterations == r2.iterations and np.array_equal(a, b)
