@@ -46,10 +46,16 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp32split", choices=["fp64", "fp32split"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_reference", "fp32split"],
+                    help="headline form of the gather: fp64 (FP64 drop-in on the cell-"
+                         "polynomial store), fp64_reference (FP64 in the reference's 16-tap "
+                         "order) or fp32split (FP32 split-index gather)")
     ap.add_argument("--small", action="store_true",
                     help="small case for profiling: the same batched launch (8 lines of "
-                         "L=2^20) on a 256-row field (3 GB of coefficients)")
+                         "L=2^20) on a 64-row field (about 3 GB of field stores)")
+    ap.add_argument("--no-poly-store", action="store_true",
+                    help="field without the FP64 cell-polynomial store: the fp64 form sums the "
+                         "16 taps in the reference's order")
     ap.add_argument("--no-edge-store", action="store_true",
                     help="field without the x-filtered FP32 copy: the split gather reads the 16 "
                          "B-spline taps per edge (the form used on lines that do not have one "
@@ -620,6 +626,24 @@ def timed(torch, fn, steps, ctx):
     return e0.elapsed_time(e1), ctx.launches() - l0
 
 
+def fp64_peak(Q, ctx):
+    """FP64 FMA instructions/s of this GPU from the library's microbenchmark
+    (best of three timed launches)."""
+    best, ms = 0.0, None
+    for _ in range(3):
+        r, m = ctx.measure_fp64_fma_rate(4096)
+        if r > best:
+            best, ms = r, m
+    return best, ms
+
+
+# FP64 instructions (DFMA + DADD + DMUL, thread level) per line point of each
+# FP64 kernel on the headline workload, from ncu's
+# smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of one
+# batched launch divided by its points (the profiles under profiles/).
+FP64_INST_PER_POINT = {"k_gradient_poly": 8.0, "k_gradient": 64.0}
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -632,45 +656,66 @@ def run_ours(args):
     import qew_gb300 as Q
 
     if args.small:
-        L, ny, n_inst = L_FULL, 256, N_INST
+        L, ny, n_inst = L_FULL, 64, N_INST
     else:
         L, ny, n_inst = L_FULL, NY_FULL, N_INST
     field = gaussian_field_gpu(torch, L, ny, XI, SEED + rank)
-    edge = 0 if args.no_edge_store else Q.QEW_STORE_FP32_EDGE
-    noise = Q.FilteredNoise(field, float(L), float(ny),
-                            store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 | edge)
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    if not args.no_edge_store:
+        store |= Q.QEW_STORE_FP32_EDGE
+    if not args.no_poly_store:
+        store |= Q.QEW_STORE_FP64_POLY
+    noise = Q.FilteredNoise(field, float(L), float(ny), store=store)
     del field
     torch.cuda.empty_cache()
     rng = np.random.default_rng(SEED + 1000 * rank)
     band = ny / n_inst
     hs_host = [np.ascontiguousarray(band * (k + 0.5) + smooth_walk(rng, L, min(8.0, band / 8), 64.0))
                for k in range(n_inst)]
-    hs = [torch.as_tensor(h, device="cuda") for h in hs_host]
-    g64 = [torch.empty_like(h) for h in hs]
+    H = torch.as_tensor(np.stack(hs_host), device="cuda")  # [n_inst, L], line k at k * L
+    G = torch.empty_like(H)
     cells = torch.empty((n_inst, L), dtype=torch.int32, device="cuda")
     fracs = torch.empty((n_inst, L), dtype=torch.float32, device="cuda")
     for k in range(n_inst):
-        c, fr = Q.split_heights(hs[k], noise)
+        c, fr = Q.split_heights(H[k], noise)
         cells[k].copy_(c)
         fracs[k].copy_(fr)
     g32 = torch.empty((n_inst, L), dtype=torch.float32, device="cuda")
     p = Q.Params(float(L), 1.0, 0.0, Q.Model.Linear)
     ctx = noise.ctx
 
-    def step_split():  # all instances in one launch
+    # The three forms of the gather on the same lines, each one step = the
+    # gradients of all n_inst lines:
+    #   fp64            FP64 drop-in: the cell-polynomial store, one batched
+    #                   persistent launch (k_gradient_poly)
+    #   fp64_reference  FP64 in the reference's 16-tap order, one launch per
+    #                   line (k_gradient)
+    #   fp32split       FP32 split-index gather on the x-filtered FP32 store,
+    #                   one batched persistent launch (k_gradient_split_persist)
+    def step_fp64():
+        Q.gradient_batch(H, p, noise, G)
+
+    def step_fp64_ref():
+        Q.gradient_batch(H, p, noise, G, precision=Q.QEW_PREC_FP64_REFERENCE)
+
+    def step_split():
         Q.gradient_split_batch(cells, fracs, p, noise, g32)
 
-    def step_fp64():
-        for k in range(n_inst):
-            Q.gradient(hs[k], p, noise, g64[k])
-
-    headline_split = args.precision == "fp32split"
-    step_main, step_other = (step_split, step_fp64) if headline_split else (step_fp64, step_split)
+    poly_kernel = "k_gradient" if args.no_poly_store else "k_gradient_poly"
+    forms = {
+        "fp64": (step_fp64, 48.0, poly_kernel, "f64"),
+        "fp64_reference": (step_fp64_ref, 48.0, "k_gradient", "f64"),
+        "fp32split": (step_split, 28.0,
+                      "k_gradient_split" if args.no_edge_store else "k_gradient_split_persist",
+                      "f32"),
+    }
+    head = args.precision
     warm = max(args.warmup, 3)
     for _ in range(warm):
-        step_main()
-        step_other()
+        for fn, _, _, _ in forms.values():
+            fn()
     torch.cuda.synchronize()
+    step_main = forms[head][0]
     clocks = ClockSampler(local)
     if not args.profile_run:
         clocks.start()  # untimed warm-up steps keep the GPU loaded while the sampler starts
@@ -686,11 +731,10 @@ def run_ours(args):
         t_ms = max_over_ranks(torch, t_ms, "cuda")
         torch.distributed.barrier()
     clk = clocks.stop() if not args.profile_run else None
-    t2_ms, launches2 = timed(torch, step_other, args.steps, ctx)
     value = whole_job_rate(ws, args.steps, n_inst, L, t_ms)
-    value_other = whole_job_rate(ws, args.steps, n_inst, L, t2_ms)
 
     peak, peak_kind = measured_peak()
+    fma_rate, fma_ms = fp64_peak(Q, ctx)
 
     def roofline(ms, nl, bpp, name):
         launch_ms = ms / max(nl, 1)
@@ -698,57 +742,90 @@ def run_ours(args):
         ach = bpp * points_per_launch / (launch_ms * 1e-3) / 1e9
         return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                 "frac": ach / peak, "traffic": None, "kernel": name, "bytes_per_point": bpp,
-                "launch_us": launch_ms * 1e3, "peak_source": peak_kind}
+                "launch_us": launch_ms * 1e3, "launches": nl, "peak_source": peak_kind}
 
-    roof_split = roofline(t_ms if headline_split else t2_ms,
-                          launches if headline_split else launches2, 28.0,
-                          "k_gradient_split" if args.no_edge_store else "k_gradient_split_persist")
-    roof_fp64 = roofline(t2_ms if headline_split else t_ms,
-                         launches2 if headline_split else launches, 48.0, "k_gradient")
-    roof_split["field_store"] = (
+    def fp64_roofline(rate, name):
+        ipp = FP64_INST_PER_POINT.get(name)
+        if ipp is None:
+            return None
+        ach = ipp * rate
+        return {"bound": "fp64", "achieved": ach / 1e9, "peak": fma_rate / 1e9,
+                "unit": "G FP64 inst/s", "frac": ach / fma_rate, "kernel": name,
+                "fp64_inst_per_point": ipp,
+                "peak_source": "measured in this run: qew_measure_fp64_fma_rate, %d CTAs x 256 "
+                               "threads x 8 independent FMA chains, CUDA events (%.2f ms)"
+                               % (8 * torch.cuda.get_device_properties(local).multi_processor_count,
+                                  fma_ms)}
+
+    # DRAM bytes (read + write) per line point of each kernel from one ncu
+    # capture of the bench's batched launch (8 lines of 2^20 points) on the
+    # small field (each point touches the same number of rows whatever the
+    # field height), scaled to the points of one launch.
+    dram_per_point = {
+        "k_gradient_split_persist": (237.686784e6 + 22.566656e6) / (8 * L_FULL),
+        "k_gradient_split": (241.858816e6 + 20.879104e6) / (8 * L_FULL),
+        "k_gradient": 53.188352e6 / L_FULL,
+    }
+    results = {}
+    for name, (fn, bpp, kern, dt) in forms.items():
+        if name == head:
+            ms, nl, val = t_ms, launches, value
+        else:
+            ms, nl = timed(torch, fn, args.steps, ctx)
+            val = whole_job_rate(ws, args.steps, n_inst, L, ms)
+        roof = roofline(ms, nl, bpp, kern)
+        pts = args.steps * n_inst * L / max(nl, 1)
+        if kern in dram_per_point:
+            roof["traffic"] = dram_per_point[kern] * pts
+        results[name] = {"value": val, "unit": UNIT, "ms_per_step": ms / args.steps,
+                         "dtype": dt, "roofline": roof,
+                         "fp64_roofline": fp64_roofline(val / max(ws, 1), kern)}
+    results["fp32split"]["roofline"]["field_store"] = (
         "FP32 coefficients: 16 taps per edge" if args.no_edge_store else
         "FP32 coefficients plus the x-filtered copy: 4 taps per edge (the same rows, so the "
         "same DRAM bytes, as 16 taps)")
-    # DRAM bytes (read + write) per line point from one ncu capture of each
-    # kernel: the split gather's batched launch (8 lines of 2^20 points, 256-row
-    # field: 237.686784 MB read + 22.566656 MB written with the x-filtered store,
-    # 241.858816 + 20.879104 MB with 16 taps per edge) and the FP64 gather on
-    # one 2^20-point line (53.188352 MB), scaled to the points of one launch
-    # (traffic grows in proportion to the points).
-    pts_split = args.steps * n_inst * L / max(launches if headline_split else launches2, 1)
-    pts_fp64 = args.steps * n_inst * L / max(launches2 if headline_split else launches, 1)
-    split_bytes = ((241.858816e6 + 20.879104e6) if args.no_edge_store else
-                   (237.686784e6 + 22.566656e6))
-    roof_split["traffic"] = split_bytes / (8 * L_FULL) * pts_split
-    roof_fp64["traffic"] = 53.188352e6 / L_FULL * pts_fp64
-
+    results["fp64"]["roofline"]["field_store"] = (
+        "FP64 coefficients: 16 taps per edge in the reference's order" if args.no_poly_store else
+        "FP64 cell polynomials of the x-filtered field: one 32-byte cell per edge (the "
+        "algorithmic 4 rows x 8 B of the reference's gather)")
     e2e = None
     cpu = None
     if not args.profile_run:
-        prec = Q.QEW_PREC_FP32_SPLIT if headline_split else Q.QEW_PREC_FP64
-        hh = torch.as_tensor(np.stack(hs_host)).pin_memory().numpy()
-        gh = torch.empty((n_inst, L), dtype=torch.float64).pin_memory().numpy()
-        for _ in range(2):
-            Q.gradient_host_batch(hh, p, noise, gh, precision=prec)
-        torch.cuda.synchronize()
-        e2e_steps = max(3, args.steps // 2)
-        if ws > 1:
-            torch.distributed.barrier()
-        t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            Q.gradient_host_batch(hh, p, noise, gh, precision=prec)
-        dt = time.perf_counter() - t0
-        if ws > 1:  # the slowest replica's time, as for the device-timed value
-            dt = max_over_ranks(torch, dt * 1e3, "cuda") * 1e-3
-        e2e = {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
-               "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
-               "call": "qew_gradient_host_batch: the step's 8 lines as FP64 pinned host heights "
-                       "in, FP64 host gradients out (uploads, gradients and downloads of "
-                       "consecutive lines overlapped)"}
+        # two sets of pinned host buffers, used in turn (256 MB per step pair:
+        # nothing of one step's host data can still sit in L2 at the next)
+        hh = [torch.as_tensor(np.stack(hs_host)).pin_memory().numpy() for _ in range(2)]
+        gh = [torch.empty((n_inst, L), dtype=torch.float64).pin_memory().numpy()
+              for _ in range(2)]
+
+        def e2e_rate(name, prec):
+            for k in range(2):
+                Q.gradient_host_batch(hh[k], p, noise, gh[k], precision=prec)
+            torch.cuda.synchronize()
+            e2e_steps = max(4, args.steps)
+            if ws > 1:
+                torch.distributed.barrier()
+            t0 = time.perf_counter()
+            for k in range(e2e_steps):
+                Q.gradient_host_batch(hh[k & 1], p, noise, gh[k & 1], precision=prec)
+            dt = time.perf_counter() - t0
+            if ws > 1:  # the slowest replica's time, as for the device-timed value
+                dt = max_over_ranks(torch, dt * 1e3, "cuda") * 1e-3
+            return {"value": ws * e2e_steps * n_inst * L / dt, "unit": UNIT,
+                    "h2d_bytes_per_step": n_inst * L * 8, "d2h_bytes_per_step": n_inst * L * 8,
+                    "call": "qew_gradient_host_batch (precision %s): the step's 8 lines as "
+                            "FP64 pinned host heights in, FP64 pinned host gradients out; the "
+                            "kernels read and write the mapped host buffers over the host link "
+                            "(no staging copies)" % name}
+
+        e2e_prec = {"fp64": Q.QEW_PREC_FP64, "fp64_reference": Q.QEW_PREC_FP64_REFERENCE,
+                    "fp32split": Q.QEW_PREC_FP32_SPLIT}
+        for name in (head,) + tuple(k for k in ("fp64", "fp32split") if k != head):
+            results[name]["e2e"] = e2e_rate(name, e2e_prec[name])
+        e2e = results[head]["e2e"]
     static = ensemble = dynamics = depinning = serving = None
     sections = set(s.strip() for s in args.sections.split(",") if s.strip())
     if not args.profile_run and sections:
-        del noise, cells, fracs, g32, g64, hs
+        del noise, cells, fracs, g32, G, H
         torch.cuda.empty_cache()
         if "static" in sections:
             log("static section")
@@ -775,17 +852,19 @@ def run_ours(args):
             cpu = cpu_gradient_rate(args.cpu_seconds)
 
     if rank == 0:
-        other = {"precision": "fp64" if headline_split else "fp32split", "value": value_other,
-                 "unit": UNIT, "ms_per_step": t2_ms / args.steps,
-                 "roofline": roof_fp64 if headline_split else roof_split}
+        if cpu is not None:
+            for name in results:
+                results[name]["cpu_baseline"] = cpu
+        head_r = results[head]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
                 "steps": args.steps, "warmup": warm, "ms_per_step": t_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32" if headline_split else "f64", "data": "synthetic",
-                "config": headline_config(L, ny, n_inst, args.precision, ws),
-                "roofline": roof_split if headline_split else roof_fp64,
+                "dtype": head_r["dtype"], "data": "synthetic",
+                "config": headline_config(L, ny, n_inst, head, ws),
+                "roofline": head_r["roofline"], "fp64_roofline": head_r["fp64_roofline"],
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-                "other_precision": other, "static": static, "ensemble": ensemble, "dynamics": dynamics,
+                "forms": {k: v for k, v in results.items() if k != head},
+                "static": static, "ensemble": ensemble, "dynamics": dynamics,
                 "depinning": depinning, "serving": serving}
         print(json.dumps(line), flush=True)
     if ws > 1:

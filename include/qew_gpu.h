@@ -80,13 +80,28 @@ enum {
  * constants w(1/2) = 1/48, 23/48, 23/48, 1/48). With it the split-form
  * gradient on such a line reads 4 values per edge instead of 16; every other
  * line and call ignores it. */
-enum { QEW_STORE_FP64 = 1, QEW_STORE_FP32 = 2, QEW_STORE_FP32_EDGE = 4 };
+enum { QEW_STORE_FP64 = 1, QEW_STORE_FP32 = 2, QEW_STORE_FP32_EDGE = 4,
+       QEW_STORE_FP64_POLY = 8 };
+/* FP64_POLY (only together with FP64) adds, for the same lines (one point
+ * per field column), the FP64 cell polynomials of the x-filtered field: for
+ * column e and row cell j the cubic V(e + 1/2, (j + t) dy), t in [0, 1), as
+ * four FP64 numbers {q0, q1, q2, v0} with dV/dy = q0 + t (q1 + t q2) and
+ * V = v0 + dy t (q0 + t (q1/2 + t q2/3)), computed once in FP64 from the
+ * prefiltered coefficients (4x the FP64 coefficient memory, 32 bytes per
+ * cell). The FP64 gradient on such a line then reads one 32-byte cell per
+ * edge and evaluates two FMAs instead of the 16-tap tensor sum. Results stay
+ * within 1e-15 of the gradient scale of the reference's order; they are not
+ * bitwise equal to it (QEW_PREC_FP64_REFERENCE keeps that order). */
 
 /* Precision of the gather in the model kernels. FP64 is the drop-in (parity)
- * form; FP32_SPLIT gathers an FP32 coefficient copy at a height split into
- * an integer cell plus an FP32 fraction, with FP32 weights and sums (no FP64
- * arithmetic); its error against FP64 is about 1e-6 of the gradient scale. */
-enum { QEW_PREC_FP64 = 0, QEW_PREC_FP32_SPLIT = 1 };
+ * form: it uses the FP64_POLY store when the field holds it and the line has
+ * one point per field column, else the reference's 16-tap sum.
+ * FP64_REFERENCE always sums the 16 taps in the reference's order
+ * (filtered_noise.h:159-176), whatever the field stores. FP32_SPLIT gathers
+ * an FP32 coefficient copy at a height split into an integer cell plus an
+ * FP32 fraction, with FP32 weights and sums (no FP64 arithmetic); its error
+ * against FP64 is about 1e-6 of the gradient scale. */
+enum { QEW_PREC_FP64 = 0, QEW_PREC_FP32_SPLIT = 1, QEW_PREC_FP64_REFERENCE = 2 };
 
 /* LbfgsParams, lbfgs.h:32-52 (same fields, same defaults), plus
  * ls_fallback (no reference counterpart; default 0 = the reference's Armijo
@@ -226,6 +241,14 @@ qew_status qew_gradient(qew_ctx *ctx, const qew_field *field,
 qew_status qew_gradient_prec(qew_ctx *ctx, const qew_field *field,
                              const double *d_h, int n, const qew_params *p,
                              int precision, double *d_grad);
+/* gradient() of `count` lines of n points on one field, stored contiguously
+ * (line k at offset k*n of d_h and d_grad), FP64 in and out (no reference
+ * counterpart: the batched form of qew_model.h:149-201). With the
+ * FP64_POLY store on a line with one point per field column the whole batch
+ * is one persistent launch; otherwise one launch per line. */
+qew_status qew_gradient_batch(qew_ctx *ctx, const qew_field *field, int count,
+                              const double *d_h, int n, const qew_params *p,
+                              int precision, double *d_grad);
 /* Host-buffer gradient: copies h_h to the device, runs the gradient and
  * copies the result back into h_grad, all on the context's stream; returns
  * after the copy back has completed. */
@@ -511,6 +534,15 @@ qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field,
                                      int precision, double *f_c,
                                      double *f_lo_out, double *f_hi_out,
                                      int *n_blocks);
+
+/* ------------------------------------------------------------ measurement */
+/* FP64 FMA instructions per second of this GPU (no reference counterpart: the
+ * roof of the FP64-pipe-bound gather). Eight resident CTAs per SM, each
+ * thread `iters` rounds of eight independent FMA chains, timed with CUDA
+ * events on the context's stream after one untimed launch; *ms_out (may be
+ * NULL) is the timed launch's duration. */
+qew_status qew_measure_fp64_fma_rate(qew_ctx *ctx, int iters, double *fma_per_s,
+                                     double *ms_out);
 
 #ifdef __cplusplus
 }

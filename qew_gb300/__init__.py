@@ -39,13 +39,14 @@ from . import _capi
 from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # noqa: F401
                     QEW_FIELD_SINCOS, QEW_FIELD_WASHBOARD, QEW_FIELD_ZERO,
                     QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT, QEW_PREC_FP32_SPLIT,
-                    QEW_PREC_FP64, QEW_RK_PLAIN, QEW_RK_RESIDENT, QEW_STORE_FP32,
-                    QEW_STORE_FP32_EDGE, QEW_STORE_FP64, QewError)
+                    QEW_PREC_FP64, QEW_PREC_FP64_REFERENCE, QEW_RK_PLAIN, QEW_RK_RESIDENT,
+                    QEW_STORE_FP32, QEW_STORE_FP32_EDGE, QEW_STORE_FP64, QEW_STORE_FP64_POLY,
+                    QewError)
 
 __all__ = [
     "Model", "Params", "FilteredNoise", "ZeroNoise", "ConstNoise", "HarmonicWell",
     "SinusoidNoise", "AnalyticNoise", "objective", "objective_trial", "gradient",
-    "gradient_host", "gradient_host_batch", "split_heights", "join_heights", "gradient_split", "gradient_split_batch",
+    "gradient_batch", "gradient_host", "gradient_host_batch", "split_heights", "join_heights", "gradient_split", "gradient_split_batch",
     "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "ensemble_minimize",
     "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
@@ -155,6 +156,15 @@ class Context:
     def synchronize(self):
         _capi.check(self.lib.qew_ctx_synchronize(self.h), self.h, "synchronize")
 
+    def measure_fp64_fma_rate(self, iters: int = 4096):
+        """(FP64 FMA instructions per second, timed ms) of this GPU."""
+        self.sync_stream()
+        rate, ms = C.c_double(), C.c_double()
+        _capi.check(self.lib.qew_measure_fp64_fma_rate(self.h, int(iters), C.byref(rate),
+                                                       C.byref(ms)),
+                    self.h, "measure_fp64_fma_rate")
+        return rate.value, ms.value
+
     def __del__(self):
         try:
             if getattr(self, "h", None):
@@ -213,7 +223,10 @@ class FilteredNoise(_Noise):
     The periodic cubic B-spline prefilter runs on the GPU. ``store`` selects
     FP64 and/or FP32 coefficient storage; QEW_STORE_FP32_EDGE (with FP32) adds
     the x-filtered copy that the split-form gradient reads on a line with one
-    point per field column (4 taps per edge instead of 16).
+    point per field column (4 taps per edge instead of 16); QEW_STORE_FP64_POLY
+    (with FP64) adds the FP64 cell polynomials of the x-filtered field, which
+    the FP64 gradient on such a line reads (one 32-byte cell and two FMAs per
+    edge instead of the 16-tap sum).
     """
 
     kind = QEW_FIELD_BSPLINE
@@ -371,6 +384,23 @@ def gradient(h, p: Params, noise: _Noise, grad=None, precision: int = QEW_PREC_F
     pc = p.c()
     _capi.check(ctx.lib.qew_gradient_prec(ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc),
                                           precision, _ptr(grad)), ctx.h, "gradient")
+    return grad
+
+
+def gradient_batch(h, p: Params, noise: _Noise, grad=None, precision: int = QEW_PREC_FP64):
+    """gradient() of every row of a contiguous [count, n] FP64 CUDA tensor,
+    one launch when the field's FP64 cell-polynomial store serves the lines."""
+    torch = _torch()
+    ctx = noise.ctx
+    ctx.sync_stream()
+    if h.dim() != 2 or not h.is_contiguous() or h.dtype != torch.float64:
+        raise ValueError("expected a contiguous float64 [count, n] tensor")
+    if grad is None:
+        grad = torch.empty_like(h)
+    pc = p.c()
+    _capi.check(ctx.lib.qew_gradient_batch(ctx.h, noise.h, h.shape[0], _ptr(h), h.shape[1],
+                                           C.byref(pc), precision, _ptr(grad)),
+                ctx.h, "gradient_batch")
     return grad
 
 

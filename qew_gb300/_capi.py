@@ -27,8 +27,8 @@ QEW_ERR_UNSUPPORTED = 6
 
 QEW_FIELD_BSPLINE, QEW_FIELD_ZERO, QEW_FIELD_CONST = 0, 1, 2
 QEW_FIELD_HARMONIC, QEW_FIELD_WASHBOARD, QEW_FIELD_SINCOS = 3, 4, 5
-QEW_STORE_FP64, QEW_STORE_FP32, QEW_STORE_FP32_EDGE = 1, 2, 4
-QEW_PREC_FP64, QEW_PREC_FP32_SPLIT = 0, 1
+QEW_STORE_FP64, QEW_STORE_FP32, QEW_STORE_FP32_EDGE, QEW_STORE_FP64_POLY = 1, 2, 4, 8
+QEW_PREC_FP64, QEW_PREC_FP32_SPLIT, QEW_PREC_FP64_REFERENCE = 0, 1, 2
 QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
 QEW_NOALLOC_MAX_N = 1048576
 QEW_RK_PLAIN, QEW_RK_RESIDENT = 0, 1
@@ -162,6 +162,8 @@ _SIGS = {
     "qew_objective_trial": (I, [VP, VP, VP, VP, D, I, C.POINTER(qew_params), PD]),
     "qew_gradient": (I, [VP, VP, VP, I, C.POINTER(qew_params), VP]),
     "qew_gradient_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
+    "qew_gradient_batch": (I, [VP, VP, I, VP, I, C.POINTER(qew_params), I, VP]),
+    "qew_measure_fp64_fma_rate": (I, [VP, I, PD, PD]),
     "qew_gradient_host": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_gradient_host_batch": (I, [VP, VP, I, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_split_heights": (I, [VP, VP, VP, I, VP, VP]),

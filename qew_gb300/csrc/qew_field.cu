@@ -11,6 +11,7 @@
 // the FFT division up to rounding, for any nx, ny, in O(nx*ny) work.
 #include "qew_internal.cuh"
 #include "qew_philox.cuh"
+#include "qew_poly.cuh"
 
 #include <cufft.h>
 
@@ -233,6 +234,8 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
         return qew_fail(ctx, QEW_ERR_INVALID, "field_create: bad arguments");
     if ((store & QEW_STORE_FP32_EDGE) && !(store & QEW_STORE_FP32))
         return qew_fail(ctx, QEW_ERR_INVALID, "field_create: QEW_STORE_FP32_EDGE needs QEW_STORE_FP32");
+    if ((store & QEW_STORE_FP64_POLY) && !(store & QEW_STORE_FP64))
+        return qew_fail(ctx, QEW_ERR_INVALID, "field_create: QEW_STORE_FP64_POLY needs QEW_STORE_FP64");
     // transposes tile 32 columns per grid row: keep both extents within the grid limit
     if (nx > 65535 * 32 || ny > 65535 * 32)
         return qew_fail(ctx, QEW_ERR_INVALID, "field_create: nx and ny must be <= %d", 65535 * 32);
@@ -256,6 +259,7 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
         qew_free_async(c64, ctx->stream);
         qew_free_async(f->coef32, ctx->stream);
         qew_free_async(f->edge32, ctx->stream);
+        qew_free_async(f->poly64, ctx->stream);
         cudaStreamSynchronize(ctx->stream);
         delete f;
         return s;
@@ -292,6 +296,12 @@ qew_status field_build(qew_ctx *ctx, const double *src, bool src_on_device, int 
         const dim3 eg((unsigned)std::min((nx + 255) / 256, 64), (unsigned)std::min(ny, 65535));
         k_edge_fp32<<<eg, 256, 0, ctx->stream>>>(c64, f->edge32, nx, ny);
         st = qew_launch_check(ctx, "edge_fp32");
+        if (st != QEW_OK) return cleanup(st);
+    }
+    if (store & QEW_STORE_FP64_POLY) {
+        if (qew_alloc_async(ctx, (void **)&f->poly64, 4 * N * sizeof(double)) != QEW_OK)
+            return cleanup(QEW_ERR_NOMEM);
+        st = qew_poly_store_build(ctx, c64, nx, ny, f->dy, f->poly64);
         if (st != QEW_OK) return cleanup(st);
     }
     e = cudaStreamSynchronize(ctx->stream);
@@ -459,11 +469,12 @@ qew_status qew_field_destroy(qew_field *f) {
     if (!f) return QEW_OK;
     cudaSetDevice(f->device);
     // the coefficients may be in use on any stream: wait for the device
-    const bool held = f->coef64 || f->coef32 || f->edge32;
+    const bool held = f->coef64 || f->coef32 || f->edge32 || f->poly64;
     if (held) cudaDeviceSynchronize();
     qew_free_async(f->coef64, f->stream);
     qew_free_async(f->coef32, f->stream);
     qew_free_async(f->edge32, f->stream);
+    qew_free_async(f->poly64, f->stream);
     if (held) cudaStreamSynchronize(f->stream);
     delete f;
     return QEW_OK;
@@ -476,6 +487,7 @@ void qew_field_release_on(qew_field *f, cudaStream_t stream) {
     qew_free_async(f->coef64, stream);
     qew_free_async(f->coef32, stream);
     qew_free_async(f->edge32, stream);
+    qew_free_async(f->poly64, stream);
     delete f;
 }
 

@@ -54,6 +54,7 @@ struct qew_field {
     double *coef64 = nullptr;  // [ny][nx], x fastest
     float *coef32 = nullptr;   // [ny][nx], x fastest
     float *edge32 = nullptr;   // [ny][nx]: coefficients filtered along x at e + 1/2
+    double *poly64 = nullptr;  // [ny][nx][4]: FP64 cell polynomials of the x-filtered field
     cudaStream_t stream = nullptr;  // stream the coefficients were allocated on
 };
 

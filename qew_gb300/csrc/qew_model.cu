@@ -11,6 +11,7 @@
 // result is bit-reproducible for a given n regardless of scheduling.
 #include "qew_internal.cuh"
 #include "qew_model_kernels.cuh"
+#include "qew_poly.cuh"
 
 namespace {
 
@@ -42,7 +43,38 @@ qew_status objective_impl(qew_ctx *ctx, const qew_field *field, const At &at, in
     return QEW_OK;
 }
 
+// Device address of host memory that the GPU can reach directly (pinned or
+// registered host memory, mapped into the device's address space), or null
+// for pageable memory. Needs the context's device current.
+const void *mapped_host_address(const void *ptr) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return a.devicePointer;
+}
+
 }  // namespace
+
+// Host-buffer gradients without copies: when both host buffers are mapped
+// (pinned) host memory, the kernels read the heights and write the
+// gradients through the host link themselves (NVLink-C2C on Grace-based
+// systems), so the transfer and the gather overlap inside one launch.
+// QEW_ERR_UNSUPPORTED (nothing done) when either buffer is pageable or not
+// 8-byte aligned.
+static qew_status gradient_mapped(qew_ctx *ctx, const qew_field *field, int count,
+                                  const double *h_h, int n, const qew_params *p, int precision,
+                                  double *h_grad) {
+    if (((uintptr_t)h_h | (uintptr_t)h_grad) & 7u) return QEW_ERR_UNSUPPORTED;
+    const double *dh = (const double *)mapped_host_address(h_h);
+    double *dg = (double *)mapped_host_address(h_grad);
+    if (!dh || !dg) return QEW_ERR_UNSUPPORTED;
+    QEW_TRY(qew_gradient_batch(ctx, field, count, dh, n, p, precision, dg));
+    QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return QEW_OK;
+}
 
 qew_status qew_gradient_enqueue(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
                                 const qew_params *p, int precision, double *d_grad) {
@@ -56,8 +88,12 @@ qew_status qew_gradient_enqueue(qew_ctx *ctx, const qew_field *field, const doub
                             "gradient: FP32 split gather needs a B-spline field stored with QEW_STORE_FP32");
         return qew_gradient_split_enqueue(ctx, field, d_h, n, p, d_grad);
     }
-    if (precision != QEW_PREC_FP64)
+    if (precision == QEW_PREC_FP64) {  // the cell-polynomial store, when it serves this line
+        const qew_status s = qew_gradient_poly_enqueue(ctx, field, 1, d_h, n, p, d_grad);
+        if (s != QEW_ERR_UNSUPPORTED) return s;
+    } else if (precision != QEW_PREC_FP64_REFERENCE) {
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient: unknown precision %d", precision);
+    }
     return qew_dispatch_noise(ctx, field, [&](auto nz) -> qew_status {
         k_gradient<decltype(nz), kGradBS><<<blocks, kGradBS, 0, ctx->stream>>>(
             d_h, n, dx, p->line_tension, p->driving_force, p->model, nz, d_grad);
@@ -90,10 +126,29 @@ qew_status qew_gradient_prec(qew_ctx *ctx, const qew_field *field, const double 
     return qew_gradient_enqueue(ctx, field, d_h, n, p, precision, d_grad);
 }
 
+qew_status qew_gradient_batch(qew_ctx *ctx, const qew_field *field, int count, const double *d_h,
+                              int n, const qew_params *p, int precision, double *d_grad) {
+    if (!ctx || !field || !p || !d_h || !d_grad || n < 1 || count < 0)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient_batch: bad arguments");
+    if (count == 0) return QEW_OK;
+    if (precision == QEW_PREC_FP64) {
+        const qew_status s = qew_gradient_poly_enqueue(ctx, field, count, d_h, n, p, d_grad);
+        if (s != QEW_ERR_UNSUPPORTED) return s;
+    }
+    for (int k = 0; k < count; ++k)
+        QEW_TRY(qew_gradient_enqueue(ctx, field, d_h + (size_t)k * n, n, p, precision,
+                                     d_grad + (size_t)k * n));
+    return QEW_OK;
+}
+
 qew_status qew_gradient_host(qew_ctx *ctx, const qew_field *field, const double *h_h, int n,
                              const qew_params *p, int precision, double *h_grad) {
     if (!ctx || !h_h || !h_grad || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_host: bad arguments");
+    QEW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (const qew_status s = gradient_mapped(ctx, field, 1, h_h, n, p, precision, h_grad);
+        s != QEW_ERR_UNSUPPORTED)
+        return s;
     const size_t bytes = sizeof(double) * (size_t)n;
     QEW_TRY(qew_scratch_reserve(ctx, 2 * bytes + 256));
     double *d_h = (double *)ctx->scratch;
@@ -116,6 +171,9 @@ qew_status qew_gradient_host_batch(qew_ctx *ctx, const qew_field *field, int cou
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_host_batch: bad arguments");
     if (count == 0) return QEW_OK;
     QEW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (const qew_status s = gradient_mapped(ctx, field, count, h_h, n, p, precision, h_grad);
+        s != QEW_ERR_UNSUPPORTED)
+        return s;
     if (!ctx->copy_in) {
         QEW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking));
         QEW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking));

@@ -1,0 +1,241 @@
+// qew_poly.cu -- FP64 gradient on the cell-polynomial store (QEW_STORE_FP64_POLY).
+//
+// gradient() (qew_model.h:149-193) of lines with one point per field column,
+// in FP64 throughout: the edge pass reads one 32-byte cell of the store per
+// edge (the x-filtered field's cubic in the row fraction, built once with the
+// field) and evaluates dV/dy with two FMAs; the per-site combine is the
+// reference's, with its factors folded:
+//   grad_i = dx (F_el,i + (dv_{i-1} + dv_i)/2 - f)
+//          = c_el d2h_i + (dx/2)(dv_{i-1} + dv_i) - dx f        (linear,
+//            c_el = -Gamma/dx, d2h_i = (h_{i-1} + h_{i+1}) - 2 h_i as the reference forms it)
+//          = Gamma (s_{i-1} - s_i) + (dx/2)(dv_{i-1} + dv_i) - dx f  (arclength).
+// The row cell and fraction of each edge midpoint come from the bits of
+// h_e + h_{e+1} when the row spacing is a power of two (qew_poly.cuh), so an
+// edge of the linear model costs 3 FP64 instructions and a site 5.
+//
+// Launch: persistent, batched (lines stored n apart), one CTA per resident
+// slot; each CTA walks tiles of kTile sites gridDim.x apart and copies the
+// next tile's heights into its spare shared buffer with cp.async while the
+// current tile's gathers are in flight. The wrap edge of each line (at
+// x = (n - 1) dx / 2, not a half-integer column) takes the 16-tap path.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+
+#include "qew_internal.cuh"
+#include "qew_poly.cuh"
+
+namespace {
+
+constexpr int kBS = 256;
+#ifndef QEW_POLY_ITEMS
+#define QEW_POLY_ITEMS 2
+#endif
+#ifndef QEW_POLY_MIN_CTAS
+#define QEW_POLY_MIN_CTAS 4
+#endif
+constexpr int kItems = QEW_POLY_ITEMS;
+constexpr int kTile = kBS * kItems;
+
+struct PolyGeom {
+    const double *poly;   // [ny][nx][4]
+    NoiseBSpline64 nz;    // 16-tap path of the wrap edge and the reference's fold
+    int n;
+    int ky;               // (h_e + h_ep) * 2^ky = midpoint in row cells, or kPolyNotPow2
+    double half_inv_dy;   // 0.5 / dy when the spacing is not a power of two
+    LineDx L;
+    double c_el;          // -Gamma / dx
+    double lt;            // Gamma
+    double half_dx, fdx;  // dx / 2, dx f
+};
+
+// dV/dy at the midpoint of edge (e, e + 1 mod n) of heights he, hep.
+__device__ __forceinline__ double poly_edge_dvdy(const PolyGeom &g, int e, double he,
+                                                 double hep) {
+    const double a = hep + he;  // the reference's (h_ip + h_i), qew_model.h:168
+    if (e + 1 < g.n) {
+        int iy;
+        double t;
+        poly_locate(a, g.ky, g.half_inv_dy, g.nz, iy, t);
+        double q0, q1, q2;
+        poly_load3(g.poly + ((size_t)iy * (size_t)g.nz.nx + (size_t)e) * 4, q0, q1, q2);
+        return poly_dvdy(q0, q1, q2, t);
+    }
+    const double xc = (double)e * 0.5 * g.L.dx;  // (i + ip) dx / 2 with ip = 0
+    return g.nz.dvdy(xc, a * 0.5);
+}
+
+// 8-byte asynchronous global -> shared copy.
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+template <bool kArc>
+__global__ void __launch_bounds__(kBS, QEW_POLY_MIN_CTAS)
+k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ grad, int count) {
+    __shared__ double s_h[2][kTile + 2];
+    __shared__ double s_dv[kTile + 1];
+    __shared__ double s_sl[kArc ? kTile + 1 : 1];
+    const int n = g.n;
+    const int per_line = (n + kTile - 1) / kTile;
+    const int t = threadIdx.x;
+    // This CTA's tiles are blockIdx.x + k * gridDim.x in line-major order;
+    // (line, index in line) advance by a fixed step, one division per CTA.
+    const int step_l = (int)gridDim.x / per_line;
+    const int step_i = (int)gridDim.x - step_l * per_line;
+    auto fetch = [&](int line, int idx, int buf) {  // a tile's heights (+ halo) into buffer buf
+        const int base = idx * kTile;
+        const int cnt = min(kTile, n - base);
+        const double *hl = h + (size_t)line * (size_t)n;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const int j = t + k * kBS;
+            if (j < cnt) cp_async8(&s_h[buf][j + 1], hl + base + j);
+        }
+        if (t == 0) {
+            cp_async8(&s_h[buf][0], hl + (base == 0 ? n - 1 : base - 1));
+        } else if (t == kBS - 1) {
+            cp_async8(&s_h[buf][cnt + 1], hl + ((base + cnt == n) ? 0 : base + cnt));
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    int line = (int)blockIdx.x / per_line;
+    int idx = (int)blockIdx.x - line * per_line;
+    if (line < count) fetch(line, idx, 0);
+    for (int buf = 0; line < count; buf ^= 1) {
+        int nline = line + step_l, nidx = idx + step_i;
+        if (nidx >= per_line) {
+            nidx -= per_line;
+            ++nline;
+        }
+        const int base = idx * kTile;
+        const int cnt = min(kTile, n - base);
+        const double *sh = s_h[buf];
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        // Barrier A: this tile's heights are in place, and every thread has
+        // left the previous tile, whose buffer may now be refilled and whose
+        // edge values may be rewritten.
+        __syncthreads();
+        if (nline < count) fetch(nline, nidx, buf ^ 1);
+        auto edge = [&](int e, int slot) {
+            const double he = sh[slot], hep = sh[slot + 1];
+            s_dv[slot] = poly_edge_dvdy(g, e, he, hep);
+            if (kArc) {
+                const double dh = g.L.div(hep - he);
+                s_sl[slot] = dh * rsqrt(1.0 + dh * dh);
+            }
+        };
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const int j = t + k * kBS;
+            if (j < cnt) edge(base + j, j + 1);
+        }
+        if (t == kBS - 1) edge(base == 0 ? n - 1 : base - 1, 0);
+        __syncthreads();  // barrier B: edge values in place
+        double *out = grad + (size_t)line * (size_t)n + base;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const int j = t + k * kBS;
+            if (j >= cnt) break;
+            const double rest = fma(g.half_dx, s_dv[j] + s_dv[j + 1], -g.fdx);
+            double gr;
+            if (kArc) {
+                gr = fma(g.lt, s_sl[j] - s_sl[j + 1], rest);
+            } else {
+                const double d2h = fma(-2.0, sh[j + 1], sh[j] + sh[j + 2]);
+                gr = fma(g.c_el, d2h, rest);
+            }
+            __stcs(out + j, gr);
+        }
+        line = nline;
+        idx = nidx;
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// {q0, q1, q2, v0} of every (row cell j, column e) from the FP64
+// coefficients c ([ny][nx]); see qew_poly.cuh for the formulas.
+__global__ void k_poly_store(const double *__restrict__ c, int nx, int ny, double inv_dy,
+                             double *__restrict__ out) {
+    const double w0 = 1.0 / 48.0, w1 = 23.0 / 48.0, s6 = 1.0 / 6.0;
+    for (int j = blockIdx.y; j < ny; j += gridDim.y) {
+        int rows[4];
+        wrap4(j, ny, rows);
+        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nx; e += gridDim.x * blockDim.x) {
+            const int em = (e == 0) ? nx - 1 : e - 1;
+            const int ep = (e + 1 == nx) ? 0 : e + 1;
+            const int ep2 = (ep + 1 == nx) ? 0 : ep + 1;
+            double E[4];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const double *r = c + (size_t)rows[b] * (size_t)nx;
+                E[b] = w0 * r[em] + w1 * r[e] + w1 * r[ep] + w0 * r[ep2];
+            }
+            double *o = out + ((size_t)j * (size_t)nx + (size_t)e) * 4;
+            o[0] = 0.5 * (E[2] - E[0]) * inv_dy;
+            o[1] = ((E[0] + E[2]) - 2.0 * E[1]) * inv_dy;
+            o[2] = 0.5 * ((E[3] - E[0]) + 3.0 * (E[1] - E[2])) * inv_dy;
+            o[3] = (E[0] + 4.0 * E[1] + E[2]) * s6;
+        }
+    }
+}
+
+}  // namespace
+
+bool qew_poly_applies(const qew_field *f, int n, const qew_params *p) {
+    return f && f->kind == QEW_FIELD_BSPLINE && f->poly64 && f->coef64 && n == f->nx &&
+           p->physical_size == f->Lx;
+}
+
+qew_status qew_poly_store_build(qew_ctx *ctx, const double *c, int nx, int ny, double dy,
+                                double *out) {
+    const dim3 grid((unsigned)std::min((nx + 255) / 256, 64), (unsigned)std::min(ny, 65535));
+    k_poly_store<<<grid, 256, 0, ctx->stream>>>(c, nx, ny, 1.0 / dy, out);
+    return qew_launch_check(ctx, "poly_store");
+}
+
+qew_status qew_gradient_poly_enqueue(qew_ctx *ctx, const qew_field *f, int count,
+                                     const double *d_h, int n, const qew_params *p,
+                                     double *d_grad) {
+    if (!qew_poly_applies(f, n, p)) return QEW_ERR_UNSUPPORTED;
+    PolyGeom g{};
+    g.poly = f->poly64;
+    g.nz = make_bspline64(f, n, p->physical_size);
+    g.n = n;
+    g.ky = poly_scale_exponent(f->dy);
+    g.half_inv_dy = 0.5 / f->dy;
+    g.L = make_line_dx(p->physical_size, n);
+    g.c_el = -p->line_tension / g.L.dx;
+    g.lt = p->line_tension;
+    g.half_dx = 0.5 * g.L.dx;
+    g.fdx = g.L.dx * p->driving_force;
+    const bool arc = (p->model == QEW_MODEL_ARCLENGTH);
+    static const int per_sm[2] = {
+        [] {
+            int v = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_gradient_poly<false>, kBS, 0) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                v = 1;
+            }
+            return std::max(1, v);
+        }(),
+        [] {
+            int v = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_gradient_poly<true>, kBS, 0) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                v = 1;
+            }
+            return std::max(1, v);
+        }()};
+    const long long tiles = (long long)((n + kTile - 1) / kTile) * count;
+    if (tiles > INT_MAX) return qew_fail(ctx, QEW_ERR_INVALID, "gradient: more than 2^31 tiles");
+    const int grid = (int)std::min<long long>(tiles, (long long)per_sm[arc ? 1 : 0] * ctx->num_sms);
+    if (arc)
+        k_gradient_poly<true><<<grid, kBS, 0, ctx->stream>>>(d_h, g, d_grad, count);
+    else
+        k_gradient_poly<false><<<grid, kBS, 0, ctx->stream>>>(d_h, g, d_grad, count);
+    return qew_launch_check(ctx, "gradient_poly");
+}

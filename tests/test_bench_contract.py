@@ -30,7 +30,7 @@ def test_reference_arm_line():
     assert d["impl"] == "reference"
     assert (d["metric"], d["unit"], d["higher_is_better"]) == (bench.METRIC, bench.UNIT, True)
     assert d["config"] == bench.headline_config(bench.L_FULL, bench.NY_FULL, bench.N_INST,
-                                                "fp32split", 1)
+                                                "fp64", 1)
     assert d["value"] > 0 and d["steps"] == 1
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]

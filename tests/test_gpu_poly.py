@@ -1,0 +1,172 @@
+"""FP64 gradient on the cell-polynomial store (QEW_STORE_FP64_POLY) against
+the FP64 oracle.
+
+Bar: energy and gradient within 1e-12 relative (to the largest magnitude of
+the compared vector), the FP64 parity bar. The store re-associates the
+reference's tensor sum, so it is not bitwise equal to the reference's order;
+against the reference-order kernel on the same field it agrees to 1e-13.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import band_limited_field, gaussian_field
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+
+def t64(a):
+    import torch
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+def npy(t):
+    return t.detach().cpu().numpy()
+
+
+def close(a, b, rtol=RTOL):
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    err = float(np.max(np.abs(np.asarray(a) - np.asarray(b))))
+    assert err <= rtol * scale, "max err %.3e vs scale %.3e" % (err, scale)
+
+
+def poly_field(Q, fld, Lx, Ly):
+    return Q.FilteredNoise(fld, Lx, Ly, store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY)
+
+
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("shape", [(1, 8, 1.0, 8.0), (2, 8, 2.0, 8.0), (3, 5, 3.0, 5.0),
+                                   (96, 40, 4.8, 1.3), (257, 33, 257.0, 33.0),
+                                   (1000, 48, 1000.0, 12.0), (4096, 64, 4096.0, 64.0)])
+def test_poly_gradient_matches_oracle(Q, O, model, shape):
+    """One point per field column, power-of-two and other row spacings,
+    heights that leave [0, Ly) on both sides (the reference's fold)."""
+    nx, ny, Lx, Ly = shape
+    fld = band_limited_field(nx, ny, Lx, Ly, 1.0, 0.3 * Ly, nx + 7 * ny)
+    f = poly_field(Q, fld, Lx, Ly)
+    of = O.BSplineField(fld, Lx, Ly, coef=f.coefficients())
+    rng = np.random.default_rng(nx + model)
+    h = rng.uniform(-1.5 * Ly, 2.5 * Ly, nx)
+    h[::7] = rng.uniform(0, Ly, h[::7].size)
+    p = Q.Params(Lx, 1.3, 0.37, Q.Model(model))
+    po = O.params(Lx, 1.3, 0.37, model)
+    go = O.gradient(h, po, of)
+    g = npy(Q.gradient(t64(h), p, f))
+    close(g, go)
+    # the reference-order kernel on the same field
+    gr = npy(Q.gradient(t64(h), p, f, precision=Q.QEW_PREC_FP64_REFERENCE))
+    close(g, gr, 1e-13)
+    close(gr, go)
+
+
+def test_poly_cell_boundaries_and_special_heights(Q, O):
+    """Heights on exact cell boundaries, zero, tiny and negative values, and
+    far outside the field: the bit-level floor/fraction agrees with the
+    reference's floor and fold (the results match the oracle to the bar)."""
+    nx, ny = 512, 32
+    Lx, Ly = float(nx), 8.0  # dy = 0.25
+    fld = gaussian_field(nx, ny, 3.0, 21)
+    f = poly_field(Q, fld, Lx, Ly)
+    of = O.BSplineField(fld, Lx, Ly, coef=f.coefficients())
+    rng = np.random.default_rng(5)
+    specials = np.array([0.0, -0.0, 5e-324, 1e-310, 1e-300, 0.125, 0.25, 0.375, 7.75, 7.999999,
+                         8.0, 8.25, -0.25, -1e-17, 1e-17, 1e6, -1e6, 0.5, 3.0, 4.0])
+    h = rng.uniform(0, Ly, nx)
+    h[: specials.size] = specials
+    h[100:200] = np.round(h[100:200] * 4) / 4       # midpoints on cell boundaries
+    for model in (0, 1):
+        p = Q.Params(Lx, 0.9, -0.2, Q.Model(model))
+        po = O.params(Lx, 0.9, -0.2, model)
+        close(npy(Q.gradient(t64(h), p, f)), O.gradient(h, po, of))
+
+
+def test_poly_batch_equals_single_lines(Q):
+    """The batched persistent launch gives every line what a per-line call
+    gives, bit for bit, for batches shorter and longer than one wave."""
+    import torch
+    nx, ny = 3000, 48
+    f = poly_field(Q, gaussian_field(nx, ny, 4.0, 2), float(nx), float(ny))
+    rng = np.random.default_rng(9)
+    for count in (1, 3, 17):
+        h = t64(ny / 2 + np.cumsum(rng.standard_normal((count, nx)), axis=1) * 0.3)
+        for model in (0, 1):
+            p = Q.Params(float(nx), 1.0, 0.1, Q.Model(model))
+            gb = Q.gradient_batch(h, p, f)
+            for k in range(count):
+                assert torch.equal(gb[k], Q.gradient(h[k].contiguous(), p, f))
+    # a field without the store: the batch is one reference-order launch per line
+    f2 = Q.FilteredNoise(gaussian_field(nx, ny, 4.0, 2), float(nx), float(ny))
+    h = t64(ny / 2 + rng.standard_normal((2, nx)))
+    p = Q.Params(float(nx), 1.0, 0.1, Q.Model.Linear)
+    gb = Q.gradient_batch(h, p, f2)
+    for k in range(2):
+        assert torch.equal(gb[k], Q.gradient(h[k].contiguous(), p, f2))
+
+
+def test_poly_other_lines_ignore_the_store(Q):
+    """A line that does not have one point per field column (n != nx, or a
+    different physical length) takes the reference-order kernel, bitwise."""
+    import torch
+    nx, ny = 600, 32
+    fld = gaussian_field(nx, ny, 3.0, 4)
+    fp = poly_field(Q, fld, float(nx), float(ny))
+    f0 = Q.FilteredNoise(fld, float(nx), float(ny))
+    rng = np.random.default_rng(1)
+    for n, P in ((500, float(nx)), (600, 300.0)):
+        h = t64(rng.uniform(0, ny, n))
+        p = Q.Params(P, 1.0, 0.0, Q.Model.Linear)
+        assert torch.equal(Q.gradient(h, p, fp), Q.gradient(h, p, f0))
+
+
+def test_poly_store_needs_fp64(Q):
+    with pytest.raises(ValueError, match="QEW_STORE_FP64_POLY needs QEW_STORE_FP64"):
+        Q.FilteredNoise(np.zeros((16, 8)), 16.0, 8.0,
+                        store=Q.QEW_STORE_FP32 | Q.QEW_STORE_FP64_POLY)
+
+
+def test_poly_full_size_line(Q, O):
+    """A 2^20-point line on a 2^20 x 64 field, both models, against the
+    OpenMP oracle on the same (downloaded) coefficients."""
+    import torch
+    n, ny = 1 << 20, 64
+    rng = np.random.default_rng(6)
+    fld = rng.standard_normal((n, ny))
+    f = poly_field(Q, fld, float(n), float(ny))
+    of = O.BSplineField(fld, float(n), float(ny), coef=f.coefficients())
+    h = 32 + np.cumsum(rng.standard_normal(n)) * 0.05
+    for model in (0, 1):
+        p = Q.Params(float(n), 1.0, 0.3, Q.Model(model))
+        g = npy(Q.gradient(t64(h), p, f))
+        close(g, O.gradient(h, O.params(float(n), 1.0, 0.3, model), of, omp=True))
+    del f
+    torch.cuda.empty_cache()
+
+
+def test_host_batch_mapped_and_copied_agree(Q):
+    """qew_gradient_host_batch with pinned host buffers runs the kernels on
+    the mapped host memory (no copies); with a pageable output it takes the
+    copy pipeline. Both give exactly the device-resident gradient, for every
+    precision."""
+    import torch
+    nx, ny = 2048, 32
+    f = Q.FilteredNoise(gaussian_field(nx, ny, 3.0, 8), float(nx), float(ny),
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY | Q.QEW_STORE_FP32)
+    rng = np.random.default_rng(12)
+    count = 5
+    h = torch.as_tensor(ny / 2 + rng.standard_normal((count, nx))).pin_memory().numpy()
+    for model in (0, 1):
+        p = Q.Params(float(nx), 1.1, 0.05, Q.Model(model))
+        for prec in (Q.QEW_PREC_FP64, Q.QEW_PREC_FP64_REFERENCE, Q.QEW_PREC_FP32_SPLIT):
+            pinned = torch.empty((count, nx), dtype=torch.float64).pin_memory().numpy()
+            Q.gradient_host_batch(h, p, f, pinned, precision=prec)
+            pageable = Q.gradient_host_batch(h, p, f, np.empty((count, nx)), precision=prec)
+            dev = npy(Q.gradient_batch(t64(h), p, f, precision=prec)) \
+                if prec != Q.QEW_PREC_FP32_SPLIT else \
+                np.stack([npy(Q.gradient(t64(h[k]), p, f, precision=prec)) for k in range(count)])
+            assert np.array_equal(pinned, dev)
+            assert np.array_equal(pageable, dev)
+            one = torch.empty(nx, dtype=torch.float64).pin_memory().numpy()
+            Q.gradient_host(h[2].copy(), p, f, one, precision=prec)
+            assert np.array_equal(one, dev[2])

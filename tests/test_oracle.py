@@ -263,6 +263,39 @@ def test_x_filtered_store_identity(O):
     assert np.max(np.abs(dvdy - dvdyo)) <= 1e-13 * np.max(np.abs(dvdyo))
 
 
+def test_cell_polynomial_store_identity(O):
+    """The FP64 cell-polynomial store's algebra: inside row cell j the
+    x-filtered interpolant at x = (e + 1/2) dx is the cubic
+    v0 + dy t (q0 + t (q1/2 + t q2/3)) with dV/dy = q0 + t (q1 + t q2), whose
+    coefficients are fixed combinations of the x sums E of rows j-1 .. j+2.
+    Evaluated that way it reproduces the oracle's 16-tap value and dV/dy (to
+    rounding; the sum's order aside), including rows that wrap."""
+    nx, ny, Lx, Ly = 64, 16, 64.0, 5.6                    # dy = 0.35: not a power of two
+    rng = np.random.default_rng(12)
+    fld = rng.standard_normal((nx, ny))
+    of = O.BSplineField(fld, Lx, Ly)
+    c = of.coef                                           # [nx][ny], y fastest
+    w = np.array([1.0, 23.0, 23.0, 1.0]) / 48.0
+    E = sum(w[a] * np.roll(c, 1 - a, axis=0) for a in range(4))
+    dx, dy = Lx / nx, Ly / ny
+    Eb = [np.roll(E, 1 - b, axis=1) for b in range(4)]    # Eb[b][e, j] = E[e, j - 1 + b]
+    q0 = 0.5 * (Eb[2] - Eb[0]) / dy
+    q1 = ((Eb[0] + Eb[2]) - 2.0 * Eb[1]) / dy
+    q2 = 0.5 * ((Eb[3] - Eb[0]) + 3.0 * (Eb[1] - Eb[2])) / dy
+    v0 = (Eb[0] + 4.0 * Eb[1] + Eb[2]) / 6.0
+    e = np.repeat(np.arange(nx - 1), 7)
+    y = rng.uniform(-2 * Ly, 3 * Ly, e.size)
+    gy = y / dy
+    iy = np.floor(gy).astype(int)
+    t = gy - iy
+    j = iy % ny
+    dv = q0[e, j] + t * (q1[e, j] + t * q2[e, j])
+    v = v0[e, j] + dy * t * (q0[e, j] + t * (0.5 * q1[e, j] + t * q2[e, j] / 3.0))
+    vo, _, dvo = O.sample(of, (e + 0.5) * dx, y)
+    assert np.max(np.abs(v - vo)) <= 1e-13 * np.max(np.abs(vo))
+    assert np.max(np.abs(dv - dvo)) <= 1e-13 * np.max(np.abs(dvo))
+
+
 def test_oracle_dynamics_known_answers(O):
     """The oracle's Langevin step against the reference's dynamics known
     answers (test_dynamics.cpp:40-161), harmonic trough k = 4, linear model,
