@@ -640,8 +640,9 @@ def fp64_peak(Q, ctx):
 # FP64 instructions (DFMA + DADD + DMUL, thread level) per line point of each
 # FP64 kernel on the headline workload, from ncu's
 # smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of one
-# batched launch divided by its points (the profiles under profiles/).
-FP64_INST_PER_POINT = {"k_gradient_poly": 8.0, "k_gradient": 64.0}
+# launch divided by its points. For k_gradient these counters leave out its
+# FP64 floor, conversions and compares, so its fraction reads low.
+FP64_INST_PER_POINT = {"k_gradient_poly": 8.0, "k_gradient": 49.15}
 
 
 def run_ours(args):
@@ -762,9 +763,10 @@ def run_ours(args):
     # small field (each point touches the same number of rows whatever the
     # field height), scaled to the points of one launch.
     dram_per_point = {
+        "k_gradient_poly": (342.752256e6 + 52.867072e6) / (8 * L_FULL),
         "k_gradient_split_persist": (237.686784e6 + 22.566656e6) / (8 * L_FULL),
         "k_gradient_split": (241.858816e6 + 20.879104e6) / (8 * L_FULL),
-        "k_gradient": 53.188352e6 / L_FULL,
+        "k_gradient": (43.320832e6 + 0.039936e6) / L_FULL,
     }
     results = {}
     for name, (fn, bpp, kern, dt) in forms.items():

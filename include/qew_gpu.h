@@ -96,8 +96,10 @@ enum { QEW_STORE_FP64 = 1, QEW_STORE_FP32 = 2, QEW_STORE_FP32_EDGE = 4,
 /* Precision of the gather in the model kernels. FP64 is the drop-in (parity)
  * form: it uses the FP64_POLY store when the field holds it and the line has
  * one point per field column, else the reference's 16-tap sum.
- * FP64_REFERENCE always sums the 16 taps in the reference's order
- * (filtered_noise.h:159-176), whatever the field stores. FP32_SPLIT gathers
+ * FP64_REFERENCE always evaluates the reference's expressions in its order
+ * with its roundings (the 16-tap sum of filtered_noise.h:159-176, true
+ * divisions, no fused multiply-adds), whatever the field stores: the
+ * reference's results bit for bit, at a higher FP64 cost. FP32_SPLIT gathers
  * an FP32 coefficient copy at a height split into an integer cell plus an
  * FP32 fraction, with FP32 weights and sums (no FP64 arithmetic); its error
  * against FP64 is about 1e-6 of the gradient scale. */
@@ -237,7 +239,9 @@ qew_status qew_objective_trial(qew_ctx *ctx, const qew_field *field,
 qew_status qew_gradient(qew_ctx *ctx, const qew_field *field,
                         const double *d_h, int n, const qew_params *p,
                         double *d_grad);
-/* gradient with the gather precision selectable (QEW_PREC_*). */
+/* gradient with the gather precision selectable (QEW_PREC_*):
+ * QEW_PREC_FP64_REFERENCE gives the reference's gradient bit for bit (its
+ * operations in its order, true divisions, no fused multiply-adds). */
 qew_status qew_gradient_prec(qew_ctx *ctx, const qew_field *field,
                              const double *d_h, int n, const qew_params *p,
                              int precision, double *d_grad);
@@ -510,7 +514,9 @@ qew_status qew_rk_block(qew_ctx *ctx, const qew_field *field, double *d_h,
 enum { QEW_RK_PLAIN = 0, QEW_RK_RESIDENT = 1 };
 /* rk_block with the form and the gather precision chosen: QEW_PREC_FP32_SPLIT
  * (resident form only) evaluates site velocities on the FP32 coefficients
- * while heights, the no-passing update and the verdicts stay FP64. */
+ * while heights, the no-passing update and the verdicts stay FP64;
+ * QEW_PREC_FP64_REFERENCE evaluates them with the reference's arithmetic bit
+ * for bit (both forms). */
 qew_status qew_rk_block_form(qew_ctx *ctx, const qew_field *field,
                              double *d_h, int n, const qew_params *p,
                              const qew_rk_params *rp, int form, int precision,
@@ -534,6 +540,29 @@ qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field,
                                      int precision, double *f_c,
                                      double *f_lo_out, double *f_hi_out,
                                      int *n_blocks);
+/* Outcome of a force bisection. Verdict of a block: 0 blocked, 1 runaway,
+ * 2 neither (max_sweeps reached; counted as not blocked, as the reference's
+ * ramp counts it, rosso_krauth.h:189-192, qew_runs.h:236-240). */
+typedef struct {
+    double f_c, f_lo, f_hi;
+    int blocks;        /* rk_block calls */
+    int n_blocked, n_runaway, n_timeout;
+    int f_hi_verdict;  /* verdict that set f_hi last: 1 runaway, 2 max_sweeps
+                          (f_c then depends on max_sweeps); 0: f_hi is the
+                          caller's bracket end */
+    long sweeps;       /* sweeps of all blocks */
+} qew_bisect_result;
+/* qew_depinning_bisect_prec reporting every block's verdict: h_verdicts (NULL
+ * or max_steps ints) receives them in order. precision QEW_PREC_FP64_REFERENCE
+ * evaluates the velocities with the reference's arithmetic bit for bit (true
+ * divisions, no fused multiply-adds), so the verdicts, f_c and the critical
+ * configuration are those of the reference's own evaluation order. */
+qew_status qew_depinning_bisect_ex(qew_ctx *ctx, const qew_field *field,
+                                   double *d_h, int n, const qew_params *p,
+                                   const qew_rk_params *rp, double f_lo,
+                                   double f_hi, double rtol, int max_steps,
+                                   int precision, qew_bisect_result *res,
+                                   int *h_verdicts);
 
 /* ------------------------------------------------------------ measurement */
 /* FP64 FMA instructions per second of this GPU (no reference counterpart: the

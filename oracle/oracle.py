@@ -100,6 +100,11 @@ def lib():
                                           C.POINTER(QoRkParams), D, D, D, I,
                                           PD, PD, PD, C.POINTER(I)]
         L.qo_depinning_bisect.restype = I
+        L.qo_depinning_bisect_ex.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
+                                             C.POINTER(QoRkParams), D, D, D, I,
+                                             PD, PD, PD, C.POINTER(I), C.POINTER(I),
+                                             C.POINTER(C.c_long)]
+        L.qo_depinning_bisect_ex.restype = I
         L.qo_philox_normals.argtypes = [C.c_uint64, C.c_uint64, I, PD]
         L.qo_fire_minimize.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
                                        C.POINTER(QoFireParams), C.POINTER(QoFireResult)]
@@ -272,6 +277,22 @@ def depinning_bisect(h: np.ndarray, p: QoParams, noise: Noise, rp: QoRkParams,
     if rc != 0:
         raise ValueError("depinning_bisect: line length must be even")
     return fc.value, flo.value, fhi.value, nb.value
+
+
+def depinning_bisect_verdicts(h: np.ndarray, p: QoParams, noise: Noise, rp: QoRkParams,
+                              f_lo, f_hi, rtol=1e-10, max_steps=200):
+    """depinning_bisect plus each block's verdict (0 blocked, 1 runaway, 2
+    max_sweeps reached) and the sweeps of all blocks together."""
+    fc, flo, fhi = D(), D(), D()
+    nb = I()
+    verdicts = (I * max(max_steps, 1))()
+    sweeps = C.c_long()
+    rc = lib().qo_depinning_bisect_ex(_p(h), h.size, C.byref(p), C.byref(noise.s), C.byref(rp),
+                                      f_lo, f_hi, rtol, max_steps, C.byref(fc), C.byref(flo),
+                                      C.byref(fhi), C.byref(nb), verdicts, C.byref(sweeps))
+    if rc != 0:
+        raise ValueError("depinning_bisect: line length must be even")
+    return fc.value, flo.value, fhi.value, list(verdicts[:nb.value]), sweeps.value
 
 
 def philox_normals(seed: int, step: int, n: int) -> np.ndarray:

@@ -964,6 +964,9 @@ int qo_rk_block(double *h, int n, const qo_params *p, const qo_noise *nz,
     double cum_adv = 0;
     for (int sweep = 0; sweep < rp->max_sweeps; ++sweep) {
         for (int color = 0; color < 2; ++color) {
+            /* sites of one colour are independent (their neighbours are of the
+             * other colour), so the threads give the serial loop's numbers */
+#pragma omp parallel for schedule(dynamic, 16) if (n >= 512)
             for (int i = color; i < n; i += 2) {
                 const int im = (i == 0) ? n - 1 : i - 1;
                 const int ip = (i + 1 == n) ? 0 : i + 1;
@@ -1015,7 +1018,20 @@ int qo_depinning_bisect(double *h, int n, const qo_params *p,
                         double f_lo, double f_hi, double rtol, int max_steps,
                         double *f_c, double *f_lo_out, double *f_hi_out,
                         int *n_blocks) {
+    return qo_depinning_bisect_ex(h, n, p, nz, rp, f_lo, f_hi, rtol, max_steps, f_c,
+                                  f_lo_out, f_hi_out, n_blocks, NULL, NULL);
+}
+
+/* The same, recording each block's verdict (0 blocked, 1 runaway, 2 neither:
+ * max_sweeps reached) in verdicts[] (max_steps entries, may be NULL) and the
+ * sweeps of every block in *sweeps (may be NULL). */
+int qo_depinning_bisect_ex(double *h, int n, const qo_params *p,
+                           const qo_noise *nz, const qo_rk_params *rp,
+                           double f_lo, double f_hi, double rtol, int max_steps,
+                           double *f_c, double *f_lo_out, double *f_hi_out,
+                           int *n_blocks, int *verdicts, long *sweeps) {
     if (n % 2 != 0) return -1;
+    if (sweeps) *sweeps = 0;
     double *work = (double *)malloc(sizeof(double) * (size_t)n);
     qo_params pp = *p;
     int steps = 0;
@@ -1025,6 +1041,8 @@ int qo_depinning_bisect(double *h, int n, const qo_params *p,
         pp.driving_force = fm;
         qo_rk_result r;
         qo_rk_block(work, n, &pp, nz, rp, &r);
+        if (verdicts) verdicts[steps] = r.blocked ? 0 : (r.runaway ? 1 : 2);
+        if (sweeps) *sweeps += r.sweeps;
         ++steps;
         if (r.blocked) {
             f_lo = fm;

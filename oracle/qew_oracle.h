@@ -169,6 +169,11 @@ int qo_depinning_bisect(double *h, int n, const qo_params *p,
                         double f_lo, double f_hi, double rtol, int max_steps,
                         double *f_c, double *f_lo_out, double *f_hi_out,
                         int *n_blocks);
+int qo_depinning_bisect_ex(double *h, int n, const qo_params *p,
+                           const qo_noise *nz, const qo_rk_params *rp,
+                           double f_lo, double f_hi, double rtol, int max_steps,
+                           double *f_c, double *f_lo_out, double *f_hi_out,
+                           int *n_blocks, int *verdicts, long *sweeps);
 
 /* ---- Philox4x32-10 counter RNG + Box-Muller normals (shared with the GPU
  * Langevin step, so the oracle can regenerate the same increments) ---- */

@@ -50,7 +50,7 @@ __all__ = [
     "LbfgsParams", "LbfgsResult", "lbfgs_minimize", "ensemble_minimize",
     "precond_apply",
     "LangevinDynamics", "RkParams", "RkResult", "rk_site_velocity", "rk_block",
-    "depinning_bisect", "Context", "default_context", "QewError", "Server",
+    "depinning_bisect", "depinning_bisect_report", "BisectResult", "Context", "default_context", "QewError", "Server",
     "StaticConfig", "StaticProfile", "static_sweep", "DynamicConfig", "DynamicSnapshot",
     "DynamicResult", "dynamic_anneal", "DepinningConfig", "DepinningStep", "DepinningResult",
     "depinning_ramp", "FireParams", "FireResult", "fire_minimize", "line_statistics",
@@ -666,6 +666,39 @@ def depinning_bisect(h, p: Params, noise: _Noise, rp: RkParams, f_lo: float, f_h
         float(rtol), int(max_steps), int(precision), C.byref(fc), C.byref(flo), C.byref(fhi),
         C.byref(nb)), ctx.h, "depinning_bisect")
     return fc.value, flo.value, fhi.value, nb.value
+
+
+@dataclass
+class BisectResult:
+    """qew_bisect_result plus the verdict of every block (0 blocked, 1
+    runaway, 2 max_sweeps reached)."""
+    f_c: float
+    f_lo: float
+    f_hi: float
+    blocks: int
+    n_blocked: int
+    n_runaway: int
+    n_timeout: int
+    f_hi_verdict: int
+    sweeps: int
+    verdicts: list
+
+
+def depinning_bisect_report(h, p: Params, noise: _Noise, rp: RkParams, f_lo: float,
+                            f_hi: float, rtol: float = 1e-10, max_steps: int = 200,
+                            precision: int = QEW_PREC_FP64) -> BisectResult:
+    """depinning_bisect with each block's verdict (qew_depinning_bisect_ex)."""
+    ctx = noise.ctx
+    ctx.sync_stream()
+    pc, rpc = p.c(), rp.c()
+    r = _capi.qew_bisect_result()
+    verdicts = (C.c_int * max(int(max_steps), 1))()
+    _capi.check(ctx.lib.qew_depinning_bisect_ex(
+        ctx.h, noise.h, _ptr(h), h.numel(), C.byref(pc), C.byref(rpc), float(f_lo), float(f_hi),
+        float(rtol), int(max_steps), int(precision), C.byref(r), verdicts),
+        ctx.h, "depinning_bisect")
+    return BisectResult(r.f_c, r.f_lo, r.f_hi, r.blocks, r.n_blocked, r.n_runaway, r.n_timeout,
+                        r.f_hi_verdict, r.sweeps, list(verdicts[:r.blocks]))
 
 
 # ------------------------------------------------------------------- FIRE

@@ -61,6 +61,11 @@ class qew_rk_result(C.Structure):
                 ("mean_h", D)]
 
 
+class qew_bisect_result(C.Structure):
+    _fields_ = [("f_c", D), ("f_lo", D), ("f_hi", D), ("blocks", I), ("n_blocked", I),
+                ("n_runaway", I), ("n_timeout", I), ("f_hi_verdict", I), ("sweeps", C.c_long)]
+
+
 class qew_fire_params(C.Structure):
     _fields_ = [("dt_max", D), ("dt_init", D), ("ftol", D), ("max_iter", I), ("n_min", I),
                 ("f_inc", D), ("f_dec", D), ("alpha_start", D), ("f_alpha", D)]
@@ -204,6 +209,9 @@ _SIGS = {
     "qew_depinning_bisect_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params),
                                       C.POINTER(qew_rk_params), D, D, D, I, I, PD, PD, PD,
                                       C.POINTER(I)]),
+    "qew_depinning_bisect_ex": (I, [VP, VP, VP, I, C.POINTER(qew_params),
+                                    C.POINTER(qew_rk_params), D, D, D, I, I,
+                                    C.POINTER(qew_bisect_result), C.POINTER(I)]),
     "qew_fire_default_params": (I, [C.POINTER(qew_fire_params)]),
     "qew_fire_minimize": (I, [VP, VP, VP, I, C.POINTER(qew_params), C.POINTER(qew_fire_params),
                               C.POINTER(qew_fire_result)]),

@@ -292,6 +292,109 @@ struct NoiseBSpline64 {
     }
 };
 
+// ------------------------------------------- reference-exact FP64 arithmetic
+// The reference is ISO C++ evaluated expression by expression: every a*b+c is
+// a rounded product and a rounded sum, every weight a true division by 6
+// (filtered_noise.h:33-62). The __d*_rn intrinsics are never contracted into
+// FMAs, so the functions below reproduce those operations bit for bit (the
+// CPU oracle is compiled with -ffp-contract=off for the same reason).
+__device__ __forceinline__ void bsw_value_ref(double t, double w[4]) {
+    const double t2 = __dmul_rn(t, t);
+    const double t3 = __dmul_rn(t2, t);
+    const double omt = __dsub_rn(1.0, t);
+    w[0] = __ddiv_rn(__dmul_rn(__dmul_rn(omt, omt), omt), 6.0);
+    w[1] = __ddiv_rn(__dadd_rn(__dsub_rn(4.0, __dmul_rn(6.0, t2)), __dmul_rn(3.0, t3)), 6.0);
+    w[2] = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(1.0, __dmul_rn(3.0, t)), __dmul_rn(3.0, t2)),
+                               __dmul_rn(3.0, t3)),
+                     6.0);
+    w[3] = __ddiv_rn(t3, 6.0);
+}
+__device__ __forceinline__ void bsw_deriv_ref(double t, double dw[4]) {
+    const double t2 = __dmul_rn(t, t);
+    const double omt = __dsub_rn(1.0, t);
+    dw[0] = __ddiv_rn(__dmul_rn(-omt, omt), 2.0);
+    dw[1] = __ddiv_rn(__dadd_rn(__dmul_rn(-12.0, t), __dmul_rn(9.0, t2)), 6.0);
+    dw[2] = __ddiv_rn(__dsub_rn(__dadd_rn(3.0, __dmul_rn(6.0, t)), __dmul_rn(9.0, t2)), 6.0);
+    dw[3] = __ddiv_rn(__dmul_rn(3.0, t2), 6.0);
+}
+
+// DeviceNoise with the reference's arithmetic exactly (filtered_noise.h:77-176):
+// the same locate, true divisions, unfused sums in the reference's order.
+struct NoiseBSpline64Ref {
+    NoiseBSpline64 b;  // coefficients, extents and spacings (its xconst is not used)
+    __device__ __forceinline__ double c(int ix, int iy) const { return b.c(ix, iy); }
+    __device__ __forceinline__ double value(double x, double y) const {
+        int ixn[4], iyn[4];
+        double fx, fy, wx[4], wy[4];
+        b.locate(x, y, ixn, iyn, fx, fy);
+        bsw_value_ref(fx, wx);
+        bsw_value_ref(fy, wy);
+        double v = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) row = __dadd_rn(row, __dmul_rn(c(ixn[a], iyn[k]), wy[k]));
+            v = __dadd_rn(v, __dmul_rn(wx[a], row));
+        }
+        return v;
+    }
+    __device__ __forceinline__ double dvdy(double x, double y) const {
+        int ixn[4], iyn[4];
+        double fx, fy, wx[4], dwy[4];
+        b.locate(x, y, ixn, iyn, fx, fy);
+        bsw_value_ref(fx, wx);
+        bsw_deriv_ref(fy, dwy);
+        double dg = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) row = __dadd_rn(row, __dmul_rn(c(ixn[a], iyn[k]), dwy[k]));
+            dg = __dadd_rn(dg, __dmul_rn(wx[a], row));
+        }
+        return __ddiv_rn(dg, b.dy);
+    }
+    __device__ __forceinline__ void sample(double x, double y, double &v, double &dvdx_,
+                                           double &dvdy_) const {
+        int ixn[4], iyn[4];
+        double fx, fy, wx[4], dwx[4], wy[4], dwy[4];
+        b.locate(x, y, ixn, iyn, fx, fy);
+        bsw_value_ref(fx, wx);
+        bsw_deriv_ref(fx, dwx);
+        bsw_value_ref(fy, wy);
+        bsw_deriv_ref(fy, dwy);
+        double vv = 0, gx = 0, gy = 0;
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            double row = 0, row_dy = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const double cc = c(ixn[a], iyn[k]);
+                row = __dadd_rn(row, __dmul_rn(cc, wy[k]));
+                row_dy = __dadd_rn(row_dy, __dmul_rn(cc, dwy[k]));
+            }
+            vv = __dadd_rn(vv, __dmul_rn(wx[a], row));
+            gx = __dadd_rn(gx, __dmul_rn(dwx[a], row));
+            gy = __dadd_rn(gy, __dmul_rn(wx[a], row_dy));
+        }
+        v = vv;
+        dvdx_ = __ddiv_rn(gx, b.dx);
+        dvdy_ = __ddiv_rn(gy, b.dy);
+    }
+};
+
+// True for the functors whose callers must evaluate the rest of the model
+// (elastic force, combine) with the reference's unfused arithmetic too.
+template <class Noise>
+struct noise_is_ref {
+    static constexpr bool value = false;
+};
+template <>
+struct noise_is_ref<NoiseBSpline64Ref> {
+    static constexpr bool value = true;
+};
+
 // Analytic potentials of the reference's tests; value()/dvdy() go through
 // sample() exactly like detail::noise_value/noise_dvdy (qew_model.h:31-46).
 struct NoiseZero {
@@ -402,6 +505,11 @@ static inline NoiseBSpline64 make_bspline64(const qew_field *f, int n = 0,
     return nz;
 }
 
+// As qew_dispatch_noise, with the B-spline kind as NoiseBSpline64Ref (the
+// reference's arithmetic bit for bit).
+template <class Fn>
+qew_status qew_dispatch_noise_ref(qew_ctx *ctx, const qew_field *f, Fn &&fn);
+
 // Calls `fn(noise_functor)` with the functor matching the field's kind.
 // Returns QEW_ERR_INVALID for an unknown kind or a B-spline field without
 // FP64 coefficients. n / physical_size describe the line (0: unknown).
@@ -423,6 +531,18 @@ qew_status qew_dispatch_noise(qew_ctx *ctx, const qew_field *f, Fn &&fn, int n =
     default:
         return qew_fail(ctx, QEW_ERR_INVALID, "unknown field kind %d", f->kind);
     }
+}
+
+template <class Fn>
+qew_status qew_dispatch_noise_ref(qew_ctx *ctx, const qew_field *f, Fn &&fn) {
+    if (f->kind == QEW_FIELD_BSPLINE) {
+        if (!f->coef64)
+            return qew_fail(ctx, QEW_ERR_INVALID,
+                            "field has no FP64 coefficients (created without "
+                            "QEW_STORE_FP64)");
+        return fn(NoiseBSpline64Ref{make_bspline64(f)});
+    }
+    return qew_dispatch_noise(ctx, f, fn);
 }
 
 // ------------------------------------------------------ block reductions

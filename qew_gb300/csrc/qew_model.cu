@@ -88,17 +88,18 @@ qew_status qew_gradient_enqueue(qew_ctx *ctx, const qew_field *field, const doub
                             "gradient: FP32 split gather needs a B-spline field stored with QEW_STORE_FP32");
         return qew_gradient_split_enqueue(ctx, field, d_h, n, p, d_grad);
     }
-    if (precision == QEW_PREC_FP64) {  // the cell-polynomial store, when it serves this line
-        const qew_status s = qew_gradient_poly_enqueue(ctx, field, 1, d_h, n, p, d_grad);
-        if (s != QEW_ERR_UNSUPPORTED) return s;
-    } else if (precision != QEW_PREC_FP64_REFERENCE) {
-        return qew_fail(ctx, QEW_ERR_INVALID, "gradient: unknown precision %d", precision);
-    }
-    return qew_dispatch_noise(ctx, field, [&](auto nz) -> qew_status {
+    auto launch = [&](auto nz) -> qew_status {
         k_gradient<decltype(nz), kGradBS><<<blocks, kGradBS, 0, ctx->stream>>>(
             d_h, n, dx, p->line_tension, p->driving_force, p->model, nz, d_grad);
         return qew_launch_check(ctx, "gradient");
-    }, n, p->physical_size);
+    };
+    if (precision == QEW_PREC_FP64_REFERENCE) return qew_dispatch_noise_ref(ctx, field, launch);
+    if (precision != QEW_PREC_FP64)
+        return qew_fail(ctx, QEW_ERR_INVALID, "gradient: unknown precision %d", precision);
+    // the cell-polynomial store, when it serves this line
+    const qew_status s = qew_gradient_poly_enqueue(ctx, field, 1, d_h, n, p, d_grad);
+    if (s != QEW_ERR_UNSUPPORTED) return s;
+    return qew_dispatch_noise(ctx, field, launch, n, p->physical_size);
 }
 
 extern "C" {

@@ -21,15 +21,18 @@ template <class Noise>
 __device__ __forceinline__ double edge_energy(const Noise &nz, int i, int ip, double hi,
                                               double hip, const LineDx &L, double lt, double f,
                                               int model) {
+    // Unfused where a contraction would change the rounding (1 + s^2, the
+    // f*h term), so the reference-exact functor reproduces its operations.
     const double dh_dx = L.div(hip - hi);
     double line_energy;
     if (model == QEW_MODEL_LINEAR)
         line_energy = lt * dh_dx * dh_dx * 0.5;
     else
-        line_energy = lt * (sqrt(1.0 + dh_dx * dh_dx) - 1.0);
+        line_energy = lt * (sqrt(__dadd_rn(1.0, __dmul_rn(dh_dx, dh_dx))) - 1.0);
     const double xc = (double)(i + ip) * 0.5 * L.dx;
     const double hc = (hip + hi) * 0.5;
-    return L.dx * (line_energy + noise_value_edge(nz, i, xc, hc) - f * hi);
+    return L.dx * __dsub_rn(__dadd_rn(line_energy, noise_value_edge(nz, i, xc, hc)),
+                            __dmul_rn(f, hi));
 }
 
 // Edge pass of gradient(), qew_model.h:163-175: dV/dy at the midpoint of edge
@@ -45,7 +48,7 @@ __device__ __forceinline__ void edge_gradient(const Noise &nz, int e, int n, dou
     sl = 0.0;
     if (arc) {
         const double dh = L.div(hep - he);
-        sl = dh / sqrt(1.0 + dh * dh);
+        sl = dh / sqrt(__dadd_rn(1.0, __dmul_rn(dh, dh)));
     }
 }
 

@@ -60,7 +60,8 @@ qew_status qew_rk_validate(qew_ctx *ctx, int n, const qew_params *p, const qew_r
 
 // Host-driven rk_block: the reference's loop structure.
 qew_status qew_rk_block_plain(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
-                              const qew_params *p, const qew_rk_params *rp, qew_rk_result *res) {
+                              const qew_params *p, const qew_rk_params *rp, qew_rk_result *res,
+                              int precision) {
     const double dx = p->physical_size / (double)n;
     QEW_TRY(qew_scratch_reserve(ctx, sizeof(double) * (size_t)n));
     double *adv = (double *)ctx->scratch;
@@ -74,11 +75,13 @@ qew_status qew_rk_block_plain(qew_ctx *ctx, const qew_field *field, double *d_h,
     const int half = n / 2;
     for (int sweep = 0; sweep < rp->max_sweeps; ++sweep) {
         for (int color = 0; color < 2; ++color) {
-            QEW_TRY(qew_dispatch_noise(ctx, field, [&](auto nz) -> qew_status {
+            auto colour = [&](auto nz) -> qew_status {
                 k_rk_colour<<<(half + kBS - 1) / kBS, kBS, 0, ctx->stream>>>(
                     nz, d_h, adv, n, dx, p->line_tension, p->driving_force, p->model, color, rk);
                 return qew_launch_check(ctx, "rk_colour");
-            }));
+            };
+            QEW_TRY(precision == QEW_PREC_FP64_REFERENCE ? qew_dispatch_noise_ref(ctx, field, colour)
+                                                          : qew_dispatch_noise(ctx, field, colour));
         }
         double total_adv;
         QEW_TRY((vec_reduce<SumF, 1, false>(ctx, n, SumF{adv}, &total_adv)));
@@ -132,19 +135,13 @@ qew_status qew_rk_block_form(qew_ctx *ctx, const qew_field *field, double *d_h, 
     QEW_TRY(qew_rk_validate(ctx, n, p, rp));
     QEW_CUDA(ctx, cudaSetDevice(ctx->device));
     if (form == QEW_RK_PLAIN) {
-        if (precision != QEW_PREC_FP64)
+        if (precision != QEW_PREC_FP64 && precision != QEW_PREC_FP64_REFERENCE)
             return qew_fail(ctx, QEW_ERR_UNSUPPORTED, "rk_block: the host-driven form is FP64 only");
-        return qew_rk_block_plain(ctx, field, d_h, n, p, rp, res);
+        return qew_rk_block_plain(ctx, field, d_h, n, p, rp, res, precision);
     }
     if (form != QEW_RK_RESIDENT) return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: unknown form");
     return qew_rk_block_resident(ctx, field, d_h, n, p, rp, precision, res);
 }
-
-qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
-                                     const qew_params *p, const qew_rk_params *rp, double f_lo,
-                                     double f_hi, double rtol, int max_steps, int precision,
-                                     double *f_c, double *f_lo_out, double *f_hi_out,
-                                     int *n_blocks);
 
 qew_status qew_depinning_bisect(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
                                 const qew_params *p, const qew_rk_params *rp, double f_lo,
@@ -159,9 +156,25 @@ qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, doubl
                                      double f_hi, double rtol, int max_steps, int precision,
                                      double *f_c, double *f_lo_out, double *f_hi_out,
                                      int *n_blocks) {
-    if (!ctx || !field || !d_h || !f_c || !(f_hi >= f_lo) || max_steps < 0)
+    if (!f_c) return qew_fail(ctx, QEW_ERR_INVALID, "depinning_bisect: bad arguments");
+    qew_bisect_result r;
+    QEW_TRY(qew_depinning_bisect_ex(ctx, field, d_h, n, p, rp, f_lo, f_hi, rtol, max_steps,
+                                    precision, &r, nullptr));
+    *f_c = r.f_c;
+    if (f_lo_out) *f_lo_out = r.f_lo;
+    if (f_hi_out) *f_hi_out = r.f_hi;
+    if (n_blocks) *n_blocks = r.blocks;
+    return QEW_OK;
+}
+
+qew_status qew_depinning_bisect_ex(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
+                                   const qew_params *p, const qew_rk_params *rp, double f_lo,
+                                   double f_hi, double rtol, int max_steps, int precision,
+                                   qew_bisect_result *res, int *h_verdicts) {
+    if (!ctx || !field || !d_h || !res || !(f_hi >= f_lo) || max_steps < 0)
         return qew_fail(ctx, QEW_ERR_INVALID, "depinning_bisect: bad arguments");
     QEW_TRY(qew_rk_validate(ctx, n, p, rp));
+    *res = qew_bisect_result{};
     double *work = nullptr;
     QEW_TRY(qew_alloc_async(ctx, (void **)&work, sizeof(double) * (size_t)n));
     qew_params pp = *p;
@@ -181,8 +194,12 @@ qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, doubl
                                           : qew_rk_block_resident(ctx, field, work, n, &pp, rp,
                                                                   precision, &r);
         if (st != QEW_OK) break;
+        const int verdict = r.blocked ? 0 : (r.runaway ? 1 : 2);
+        if (h_verdicts) h_verdicts[steps] = verdict;
         ++steps;
-        if (r.blocked) {
+        res->sweeps += r.sweeps;
+        if (verdict == 0) {
+            ++res->n_blocked;
             f_lo = fm;
             e = cudaMemcpyAsync(d_h, work, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice,
                                 ctx->stream);
@@ -191,16 +208,21 @@ qew_status qew_depinning_bisect_prec(qew_ctx *ctx, const qew_field *field, doubl
                 break;
             }
         } else {
+            if (verdict == 1)
+                ++res->n_runaway;
+            else
+                ++res->n_timeout;
+            res->f_hi_verdict = verdict;
             f_hi = fm;
         }
     }
     qew_free_async(work, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
     if (st != QEW_OK) return st;
-    *f_c = 0.5 * (f_lo + f_hi);
-    if (f_lo_out) *f_lo_out = f_lo;
-    if (f_hi_out) *f_hi_out = f_hi;
-    if (n_blocks) *n_blocks = steps;
+    res->f_c = 0.5 * (f_lo + f_hi);
+    res->f_lo = f_lo;
+    res->f_hi = f_hi;
+    res->blocks = steps;
     return QEW_OK;
 }
 

@@ -14,7 +14,10 @@ inline RkP rkp_from(const qew_rk_params *rp) {
     return RkP{rp->dstep, rp->max_advance, rp->root_tol, rp->sweep_tol, rp->runaway, rp->max_sweeps};
 }
 
-// rk_site_velocity, rosso_krauth.h:51-82: exactly -gradient_i.
+// rk_site_velocity, rosso_krauth.h:51-82: exactly -gradient_i. Every
+// expression that a contraction could change (1 + s^2) is unfused, and the
+// others round the same either way (2*hi and 0.5*x are exact), so with the
+// reference-exact functor the velocity is the reference's bit for bit.
 template <class Noise>
 __device__ __forceinline__ double rk_site_velocity(const Noise &nz, int i, int n, double dx,
                                                    double lt, double f, int model, double hi,
@@ -27,7 +30,10 @@ __device__ __forceinline__ double rk_site_velocity(const Noise &nz, int i, int n
     } else {
         const double dhr = (hr - hi) / dx;
         const double dhl = (hi - hl) / dx;
-        line_force = lt * (dhl / sqrt(1.0 + dhl * dhl) - dhr / sqrt(1.0 + dhr * dhr)) / dx;
+        line_force = lt *
+                     (dhl / sqrt(__dadd_rn(1.0, __dmul_rn(dhl, dhl))) -
+                      dhr / sqrt(__dadd_rn(1.0, __dmul_rn(dhr, dhr)))) /
+                     dx;
     }
     const double xcl = (double)(im + i) * 0.5 * dx;
     const double hcl = (hl + hi) * 0.5;
@@ -204,7 +210,10 @@ __device__ __forceinline__ double rk_site_velocity_pair(const Noise &nz, int i, 
     } else {
         const double dhr = (hr - hi) / dx;
         const double dhl = (hi - hl) / dx;
-        line_force = lt * (dhl / sqrt(1.0 + dhl * dhl) - dhr / sqrt(1.0 + dhr * dhr)) / dx;
+        line_force = lt *
+                     (dhl / sqrt(__dadd_rn(1.0, __dmul_rn(dhl, dhl))) -
+                      dhr / sqrt(__dadd_rn(1.0, __dmul_rn(dhr, dhr)))) /
+                     dx;
     }
     const double xc = lane ? (double)(i + ip) * 0.5 * dx : (double)(im + i) * 0.5 * dx;
     const double hc = lane ? (hi + hr) * 0.5 : (hl + hi) * 0.5;

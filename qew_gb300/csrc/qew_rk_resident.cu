@@ -186,6 +186,9 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
             return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: FP32 storage needs QEW_STORE_FP32");
         return launch(make_split32(field, n, p->physical_size));
     }
+    if (precision == QEW_PREC_FP64_REFERENCE) return qew_dispatch_noise_ref(ctx, field, launch);
+    if (precision != QEW_PREC_FP64)
+        return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: unknown precision %d", precision);
     return qew_dispatch_noise(ctx, field, launch, n, p->physical_size);
 }
 
@@ -194,6 +197,6 @@ qew_status qew_rk_block_dispatch(qew_ctx *ctx, const qew_field *field, double *d
                                  qew_rk_result *res) {
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
-    if (!coop) return qew_rk_block_plain(ctx, field, d_h, n, p, rp, res);
+    if (!coop) return qew_rk_block_plain(ctx, field, d_h, n, p, rp, res, QEW_PREC_FP64);
     return qew_rk_block_resident(ctx, field, d_h, n, p, rp, QEW_PREC_FP64, res);
 }
