@@ -514,13 +514,21 @@ def run_depinning(args, Q, torch):
                 break
             f_lo, h_lo = fk, h.clone()
             k += 1
-        res = {"ramp_blocks": blocks, "ramp_sweeps": sweeps, "f_lo": f_lo, "f_hi": f_hi}
+        res = {"ramp_blocks": blocks, "ramp_sweeps": sweeps, "f_lo": f_lo, "f_hi": f_hi,
+               "ramp_end_verdict": None if f_hi is None else
+               ("runaway" if r.runaway else "max_sweeps")}
         if f_lo is not None and f_hi is not None:
-            fc, flo, fhi, nb = Q.depinning_bisect(h_lo, Q.Params(float(n), 1.0, 0.0, Q.Model.Linear),
-                                                  fld, rp, f_lo, f_hi, rtol=1e-10, max_steps=64,
-                                                  precision=prec)
+            br = Q.depinning_bisect_report(h_lo, Q.Params(float(n), 1.0, 0.0, Q.Model.Linear),
+                                           fld, rp, f_lo, f_hi, rtol=1e-10, max_steps=64,
+                                           precision=prec)
             torch.cuda.synchronize()
-            res.update({"f_c": fc, "bracket": [flo, fhi], "bisect_blocks": nb,
+            res.update({"f_c": br.f_c, "bracket": [br.f_lo, br.f_hi], "bisect_blocks": br.blocks,
+                        "bisect_sweeps": br.sweeps,
+                        "verdicts": {"blocked": br.n_blocked, "runaway": br.n_runaway,
+                                     "max_sweeps": br.n_timeout},
+                        "f_hi_set_by": {0: "ramp", 1: "runaway", 2: "max_sweeps"}[br.f_hi_verdict],
+                        "f_c_limited_by_max_sweeps": br.f_hi_verdict == 2 or
+                        (br.f_hi_verdict == 0 and not r.runaway),
                         "mean_h_critical": float(h_lo.mean())})
             crit[name] = h_lo
         res["wall_s"] = time.perf_counter() - t0

@@ -169,6 +169,14 @@ qew_status qew_ctx_destroy(qew_ctx *ctx);
 /* cuda_stream is a cudaStream_t (NULL = legacy default stream). */
 qew_status qew_ctx_set_stream(qew_ctx *ctx, void *cuda_stream);
 qew_status qew_ctx_synchronize(qew_ctx *ctx);
+/* Limits of the grid barriers in this context's later persistent cooperative
+ * launches (Langevin run, Rosso-Krauth sweeps; no reference counterpart): a
+ * wait gives up after max_polls polls of about 64 ns (<= 0: the default
+ * 2^26) and the launch returns QEW_ERR_TIMEOUT. skip_block >= 0 makes that
+ * CTA leave at its first barrier without arriving, so the others' waits run
+ * out: a fault for tests of the timeout path (-1: none). */
+qew_status qew_ctx_set_barrier_limits(qew_ctx *ctx, long long max_polls,
+                                      int skip_block);
 const char *qew_last_error(const qew_ctx *ctx);
 /* Number of this library's kernels launched through ctx so far. */
 uint64_t qew_ctx_launch_count(const qew_ctx *ctx);
@@ -307,9 +315,12 @@ qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *field,
  * every GPU loading this library holds until exit; lines longer than
  * QEW_NOALLOC_MAX_N edges return QEW_ERR_INVALID. The field's device must be
  * the current device. The first call on each device looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture. All calls share the array: calls that overlap on the GPU
- * race and must be serialised by the caller. */
+ * device address (cudaGetSymbolAddress) and keeps it for that device's
+ * current context; make that first call before any stream capture. A call
+ * after the context was destroyed and created again (cudaDeviceReset) sees a
+ * new context and looks the address up again; fields do not survive such a
+ * reset, so create them anew first. All calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller. */
 #define QEW_NOALLOC_MAX_N 1048576
 qew_status qew_objective_noalloc(const qew_field *field, const double *d_h,
                                  int n, const qew_params *p, double *d_out,

@@ -156,6 +156,12 @@ class Context:
     def synchronize(self):
         _capi.check(self.lib.qew_ctx_synchronize(self.h), self.h, "synchronize")
 
+    def set_barrier_limits(self, max_polls: int = 0, skip_block: int = -1):
+        """Grid-barrier poll limit (0: default) and a CTA that skips its
+        arrival (-1: none) for this context's later persistent launches."""
+        _capi.check(self.lib.qew_ctx_set_barrier_limits(self.h, int(max_polls), int(skip_block)),
+                    self.h, "set_barrier_limits")
+
     def measure_fp64_fma_rate(self, iters: int = 4096):
         """(FP64 FMA instructions per second, timed ms) of this GPU."""
         self.sync_stream()

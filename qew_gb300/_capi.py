@@ -169,6 +169,7 @@ _SIGS = {
     "qew_gradient_prec": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_gradient_batch": (I, [VP, VP, I, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_measure_fp64_fma_rate": (I, [VP, I, PD, PD]),
+    "qew_ctx_set_barrier_limits": (I, [VP, C.c_longlong, I]),
     "qew_gradient_host": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_gradient_host_batch": (I, [VP, VP, I, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_split_heights": (I, [VP, VP, VP, I, VP, VP]),

@@ -139,6 +139,13 @@ qew_status qew_ctx_set_stream(qew_ctx *ctx, void *cuda_stream) {
     return QEW_OK;
 }
 
+qew_status qew_ctx_set_barrier_limits(qew_ctx *ctx, long long max_polls, int skip_block) {
+    if (!ctx || skip_block < -1) return QEW_ERR_INVALID;
+    ctx->barrier_polls = max_polls > 0 ? max_polls : (1LL << 26);
+    ctx->barrier_skip = skip_block;
+    return QEW_OK;
+}
+
 qew_status qew_ctx_synchronize(qew_ctx *ctx) {
     if (!ctx) return QEW_ERR_INVALID;
     QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -38,6 +38,11 @@ struct qew_ctx {
     // kernels; 0 = every resident slot of the GPU. Contexts that share the GPU
     // (the server's workers) take a share each.
     int warp_cap = 0;
+    // grid-barrier limits of this context's cooperative kernels: polls before
+    // a wait gives up, and a CTA that skips its arrival (-1: none; a fault
+    // that tests inject to make the waits run out)
+    long long barrier_polls = 1LL << 26;
+    int barrier_skip = -1;
     std::string last_error;
     // copy streams and slot events of the host-buffer batch pipeline
     // (created on first use)

@@ -254,7 +254,7 @@ qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h
     QEW_CUDA(ctx, cudaMemcpyAsync(d_drift, h_drift, (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
     QEW_CUDA(ctx, cudaMemcpyAsync(d_diff, h_diff, (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
     QEW_CUDA(ctx, cudaMemcpyAsync(d_rs, rs.data(), (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
-    QEW_CUDA(ctx, cudaMemsetAsync(sync, 0, sizeof(GridSync), ctx->stream));
+    QEW_TRY(qew_gridsync_init(ctx, sync));
     LineDx L = make_line_dx(p->physical_size, n);
     double lt = p->line_tension, fd = p->driving_force;
     int model = p->model;

@@ -19,6 +19,8 @@
 // of every call (the partials are rewritten before they are read); calls that
 // overlap on the GPU (different streams, or host threads) race on the array
 // and must be serialised by the caller.
+#include <cuda.h>  // driver types only: the two driver calls are resolved at run time
+
 #include <mutex>
 
 #include "qew_internal.cuh"
@@ -34,23 +36,62 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxBlocks + 32];
 
 std::mutex g_setup_mu;
-double *g_scratch_ptr[kMaxDevices] = {};
+struct ScratchSlot {
+    double *ptr = nullptr;
+    unsigned long long ctx_id = 0;  // the context the address belongs to
+};
+ScratchSlot g_scratch[kMaxDevices];
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId ids are
+// never reused within a process), through driver entry points looked up once.
+bool current_context_id(unsigned long long *id) {
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {  // under g_setup_mu
+        void *a = nullptr, *b = nullptr;
+        cudaDriverEntryPointQueryResult qa{}, qb{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault,
+                                             &qa) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) ==
+                cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess && qb == cudaDriverEntryPointSuccess) {
+            get_current = (GetCurrent)a;
+            get_id = (GetId)b;
+        }
+        cudaGetLastError();
+        resolved = true;
+    }
+    CUcontext c = nullptr;
+    return get_current && get_id && get_current(&c) == CUDA_SUCCESS && c &&
+           get_id(c, id) == CUDA_SUCCESS;
+}
 
 // The array's name is only a host-side stand-in: its device address is looked
-// up once per device, with that device current, and passed to the kernel.
+// up with the device current, once per device and context, and passed to the
+// kernel. A device whose context was destroyed and created again (after
+// cudaDeviceReset, say) has a new context id, so its address is looked up
+// again instead of reusing the old one.
 qew_status scratch_address(int device, double **out) {
     if (device < 0 || device >= kMaxDevices) return QEW_ERR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[device]) {
+    ScratchSlot &slot = g_scratch[device];
+    unsigned long long id = 0;
+    bool have_id = current_context_id(&id);
+    if (!slot.ptr || !have_id || slot.ctx_id != id) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             cudaGetLastError();
             return QEW_ERR_CUDA;
         }
-        g_scratch_ptr[device] = (double *)p;
+        if (!have_id) have_id = current_context_id(&id);  // the look-up made the context
+        slot.ptr = (double *)p;
+        slot.ctx_id = have_id ? id : 0;
     }
-    *out = g_scratch_ptr[device];
+    *out = slot.ptr;
     return QEW_OK;
 }
 

@@ -164,7 +164,7 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
         GridSync *sync = (GridSync *)(base + off_sync);
         qew_rk_result *d_res = (qew_rk_result *)(base + off_res);
         QEW_CUDA(ctx, cudaMemsetAsync(adv, 0, (size_t)n * sizeof(double), ctx->stream));
-        QEW_CUDA(ctx, cudaMemsetAsync(sync, 0, sizeof(GridSync), ctx->stream));
+        QEW_TRY(qew_gridsync_init(ctx, sync));
         double lt = p->line_tension, fd = p->driving_force;
         int model = p->model;
         void *args[] = {(void *)&nz, (void *)&d_h, (void *)&adv, (void *)&n, (void *)&dx,

@@ -275,6 +275,10 @@ qew_status qew_depinning_ramp(qew_ctx *ctx, const qew_field *field, const qew_de
         !std::isfinite(c->f_step) || !std::isfinite(c->f_max))
         return qew_fail(ctx, QEW_ERR_INVALID, "depinning_ramp: bad arguments");
     if (c->nx % 2) return qew_fail(ctx, QEW_ERR_ODD_LENGTH, "rk_block: n must be even");
+    // The force loop k * f_step <= f_max (qew_runs.h:224-227) ends only for
+    // f_step > 0 (or when it never starts, f_max < 0); bound its length.
+    if (c->f_max >= 0 && !(c->f_step > 0))
+        return qew_fail(ctx, QEW_ERR_INVALID, "depinning_ramp: need f_step > 0 (f_max >= 0)");
     if (c->f_step > 0 && c->f_max / c->f_step > 1e9)
         return qew_fail(ctx, QEW_ERR_INVALID, "depinning_ramp: more than 1e9 forces");
     const double line_tension = larkin_tension(c->pinning_length_over_xi, c->amplitude);

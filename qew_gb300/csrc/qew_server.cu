@@ -292,8 +292,9 @@ qew_status qew_server_submit(qew_server *s, const qew_request *req, uint64_t *id
     if (req->kind == QEW_REQ_LANGEVIN && (req->steps < 0 || !(req->dt > 0) || req->temperature < 0))
         return QEW_ERR_INVALID;
     if (req->kind == QEW_REQ_DEPINNING &&
-        (req->n % 2 || !(req->f_step > 0) || req->max_sweeps < 1 || !(req->bisect_rtol > 0)))
-        return QEW_ERR_INVALID;
+        (req->n % 2 || !(req->f_step > 0) || req->max_sweeps < 1 || !(req->bisect_rtol > 0) ||
+         !std::isfinite(req->f_max) || req->f_max / req->f_step > 1e9))
+        return QEW_ERR_INVALID;  // the ramp's force count is bounded as qew_depinning_ramp's
     const double est = request_bytes(*req);
     if (est > s->budget) return QEW_ERR_NOMEM;  // could never be admitted
     {

@@ -184,6 +184,20 @@ def test_depinning_odd_length_rejected(Q):
         Q.depinning_ramp(c, Q.SinusoidNoise())
 
 
+@pytest.mark.parametrize("f_step", [0.0, -0.1, float("nan")])
+def test_depinning_unbounded_ramp_rejected(Q, f_step):
+    """k * f_step <= f_max never ends for f_step <= 0 (f_max >= 0): rejected
+    instead of ramping forever; f_max < 0 runs no force at all."""
+    rp = Q.RkParams(0.01, 1.0, 1e-10, 1e-9, 2.0, 100)
+    with pytest.raises(ValueError, match="f_step|bad arguments"):
+        Q.depinning_ramp(Q.DepinningConfig(nx=8, ny=8, f_step=f_step, f_max=1.0, rp=rp),
+                         Q.SinusoidNoise())
+    if f_step == 0.0:
+        r = Q.depinning_ramp(Q.DepinningConfig(nx=8, ny=8, f_step=f_step, f_max=-1.0, rp=rp),
+                             Q.SinusoidNoise())
+        assert r.steps == [] and r.f_c_upper_bound == -1
+
+
 def _run(exe, *args, cwd):
     from qew_gb300 import build
     r = subprocess.run([build.executable(exe), *args], capture_output=True, text=True, cwd=cwd,

@@ -76,5 +76,9 @@ def test_budget_admission_and_limits(Q):
             srv.submit(kind=0, n=4096, rows=256, xi=4.0, seed=1)
         with pytest.raises(ValueError):
             srv.submit(kind=2, n=513, rows=64, xi=4.0, seed=1)
+        # a force ramp of more than 1e9 steps would hold a worker for ever
+        with pytest.raises(ValueError):
+            srv.submit(kind=2, n=512, rows=64, xi=4.0, seed=1, f_step=1e-12, f_max=40.0,
+                       bisect_rtol=1e-3, max_sweeps=100)
     finally:
         srv.close()
