@@ -48,8 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp64_reference", "fp32split"],
                     help="headline form of the gather: fp64 (FP64 drop-in on the cell-"
-                         "polynomial store), fp64_reference (FP64 in the reference's 16-tap "
-                         "order) or fp32split (FP32 split-index gather)")
+                         "polynomial store), fp64_reference (FP64 with the reference's "
+                         "arithmetic bit for bit) or fp32split (FP32 split-index gather)")
     ap.add_argument("--small", action="store_true",
                     help="small case for profiling: the same batched launch (8 lines of "
                          "L=2^20) on a 64-row field (about 3 GB of field stores)")
@@ -67,10 +67,15 @@ def parse():
                     help="lines of the batched-statics section (0 skips it)")
     ap.add_argument("--ensemble-ref", type=int, default=16,
                     help="lines timed with the plain one-line-per-launch form")
-    ap.add_argument("--sections", default="static,ensemble,dynamics,depinning,serving",
+    ap.add_argument("--sections", default="refshape,static,ensemble,dynamics,depinning,serving",
                     help="extra configurations reported beside the headline")
+    ap.add_argument("--refshape-cpu-reps", type=int, default=20,
+                    help="oracle calls per kernel on one core in the reference-shape section "
+                         "(four times as many on all cores)")
     ap.add_argument("--dyn-steps", type=int, default=100000)
     ap.add_argument("--dyn-plain-steps", type=int, default=2000)
+    ap.add_argument("--dyn-cpu-steps", type=int, default=400,
+                    help="oracle Langevin steps timed for the dynamics section's CPU baseline")
     ap.add_argument("--dep-size", type=int, default=2048,
                     help="line length and field size of the depinning section (16384: C2)")
     ap.add_argument("--dep-max-sweeps", type=int, default=20000,
@@ -437,17 +442,112 @@ def run_ensemble(args, Q, torch):
             "speedup_vs_plain": rate / plain_rate}
 
 
+# ------------------------------------------- the reference's benchmark shape
+def run_reference_shape(args, Q, torch):
+    """The reference's own timing harness (executables/benchmark/main.cpp:19-72):
+    the seeded FilteredNoise(262144, 64, Lx = 256, Ly = 1, A = 1, xi = 0.1,
+    seed 1), Params{Lx, Gamma = 1, f = 0.1, arclength}, h = Ly/2, one warm-up
+    gradient, then 200 gradient() calls, 200 objective() calls and 200
+    LangevinDynamics::step(0.01, 0.01) calls, ms per call. The reference
+    publishes 26.5 ms (gradient) and 34.4 ms (step) on one core
+    (docs/fix_plan.md:12-13). GPU: FP64 on the cell-polynomial store (the
+    line has one point per field column) and in the reference's exact
+    arithmetic; CPU: the oracle on one core and on all cores (the step draws
+    its normals from the same Philox stream as the GPU's step)."""
+    from oracle import oracle as O
+    nx, ny, Lx, Ly, reps = 262144, 64, 256.0, 1.0, 200
+    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY
+    f = Q.FilteredNoise.seeded(nx, ny, Lx, Ly, 1.0, 0.1, 0.1, 1, store=store)
+    p = Q.Params(Lx, 1.0, 0.1, Q.Model.Arclength)
+    h = torch.full((nx,), 0.5 * Ly, dtype=torch.float64, device="cuda")
+    g = torch.empty_like(h)
+    stream = torch.cuda.current_stream()
+
+    def gpu_ms(fn, n):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    out = {"workload": "FilteredNoise(262144, 64, 256, 1, 1, 0.1, 0.1, seed 1), arclength, "
+                       "Gamma=1, f=0.1, h=Ly/2; 200 calls each (benchmark/main.cpp)",
+           "unit": "ms per call",
+           "published_reference_1core": {"gradient": 26.5, "step": 34.4,
+                                         "source": "docs/fix_plan.md:12-13 (Kokkos Serial)"}}
+    gpu = {}
+    gpu["gradient_fp64"] = gpu_ms(lambda: Q.gradient(h, p, f, g), reps)
+    gpu["gradient_fp64_reference_exact"] = gpu_ms(
+        lambda: Q.gradient(h, p, f, g, precision=Q.QEW_PREC_FP64_REFERENCE), reps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        Q.objective(h, p, f)  # returns the energy to the host, as the reference does
+    gpu["objective_fp64"] = 1e3 * (time.perf_counter() - t0) / reps
+    dyn = Q.LangevinDynamics(nx, 7)
+    hs = h.clone()
+    gpu["step_fp64"] = gpu_ms(lambda: dyn.step(hs, p, f, 0.01, 0.01), reps)
+    out["gpu"] = gpu
+    # the oracle on the same coefficients
+    of = O.BSplineField(None, Lx, Ly, coef=f.coefficients())
+    op = O.params(Lx, 1.0, 0.1, 1)
+    hh = np.full(nx, 0.5 * Ly)
+    go = np.empty(nx)
+    work = (np.empty(nx), np.empty(nx))
+    cpu = {}
+    nthreads = O.omp_max_threads()
+    for label, threads, nrep in (("1core", 1, max(3, args.refshape_cpu_reps)),
+                                 ("all_cores", nthreads, 4 * max(3, args.refshape_cpu_reps))):
+        O.set_threads(threads)
+        par = threads > 1
+        O.gradient(hh, op, of, omp=par, out=go)
+        t0 = time.perf_counter()
+        for _ in range(nrep):
+            O.gradient(hh, op, of, omp=par, out=go)
+        tg = 1e3 * (time.perf_counter() - t0) / nrep
+        t0 = time.perf_counter()
+        for _ in range(nrep):
+            O.objective(hh, op, of, omp=par)
+        to = 1e3 * (time.perf_counter() - t0) / nrep
+        hs_c = hh.copy()
+        t0 = time.perf_counter()
+        for k in range(nrep):
+            O.langevin_step_philox(hs_c, op, of, 0.01, 0.01, 7, k, omp=par, work=work)
+        ts = 1e3 * (time.perf_counter() - t0) / nrep
+        cpu[label] = {"threads": threads, "calls": nrep, "gradient": tg, "objective": to,
+                      "step": ts}
+    O.set_threads(nthreads)
+    out["cpu_oracle"] = cpu
+    # the GPU's gradient against the oracle's on this field
+    gq = Q.gradient(h, p, f).cpu().numpy()
+    O.gradient(hh, op, of, omp=True, out=go)
+    out["gradient_max_rel_diff_vs_oracle"] = float(np.max(np.abs(gq - go)) / np.max(np.abs(go)))
+    out["speedup_gradient_vs_1core"] = cpu["1core"]["gradient"] / gpu["gradient_fp64"]
+    out["speedup_step_vs_1core"] = cpu["1core"]["step"] / gpu["step_fp64"]
+    out["value"] = gpu["gradient_fp64"]
+    return out
+
+
 # ------------------------------------------------------------ dynamics (C1)
 def run_dynamics(args, Q, torch):
     """Annealed overdamped Langevin: L = 65536, 65536 x 4096 field (xi = 4
     cells, seed 1), arclength, f = 0.5, Gamma = 1, T from 0.5 to 0 linearly
     over the steps, dt = 0.01 (drift = dt, diff = sqrt(2 T dt)), Philox
-    increments of seed 1; FP64 and FP32-gather runs in one device-resident
-    launch each, and the plain per-step form (gradient + update launches) on
-    the first steps."""
+    increments of seed 1. Device-resident runs (one launch each): FP64 in the
+    reference's 16-tap order, FP64 on the cell-polynomial store (the line has
+    one point per field column), FP32 split gather; the plain per-step form
+    (gradient + update launches) on the first steps; and the CPU oracle's
+    step (the same Philox increments, all host cores) on a bounded sample."""
+    from oracle import oracle as O
     n, ny, K = 65536, 4096, args.dyn_steps
-    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
-    f = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 1, store=store)
+    f = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 1,
+                                  store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32 |
+                                  Q.QEW_STORE_FP64_POLY)
+    f16 = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 1,
+                                    store=Q.QEW_STORE_FP64)
     p = Q.Params(float(n), 1.0, 0.5, Q.Model.Arclength)
     dt = 0.01
     T = 0.5 * (1.0 - np.arange(K) / K)
@@ -455,28 +555,53 @@ def run_dynamics(args, Q, torch):
     diff = np.sqrt(2.0 * T * dt)
     out = {"metric": "Langevin steps/s (L=65536)", "unit": "steps/s", "steps": K,
            "workload": "L=65536, 65536x4096 field xi=4, arclength, f=0.5, T 0.5->0, dt=0.01"}
-    for name, prec in (("fp64", Q.QEW_PREC_FP64), ("fp32split", Q.QEW_PREC_FP32_SPLIT)):
+    finals = {}
+    for name, fld, prec in (("fp64", f16, Q.QEW_PREC_FP64), ("fp64_poly", f, Q.QEW_PREC_FP64),
+                            ("fp32split", f, Q.QEW_PREC_FP32_SPLIT)):
         h = torch.full((n,), 0.5 * ny, dtype=torch.float64, device="cuda")
         dyn = Q.LangevinDynamics(n, 1)
-        dyn.run(h, p, f, drift[:10], diff[:10], precision=prec)  # warm-up
+        dyn.run(h.clone(), p, fld, drift[:10], diff[:10], precision=prec)  # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        dyn.run(h, p, f, drift, diff, precision=prec)
+        dyn.run(h, p, fld, drift, diff, precision=prec)
         torch.cuda.synchronize()
         dt_s = time.perf_counter() - t0
+        finals[name] = h
         out[name] = {"value": K / dt_s, "points_per_s": K * n / dt_s, "wall_s": dt_s,
                      "final_mean_h": float(h.mean()), "final_std_h": float(h.std())}
+    out["fp64_poly"]["vs_fp64_16tap"] = {
+        "max_abs_h_diff": float((finals["fp64_poly"] - finals["fp64"]).abs().max()),
+        "roughness_rel_diff": abs(out["fp64_poly"]["final_std_h"] - out["fp64"]["final_std_h"])
+        / out["fp64"]["final_std_h"]}
     Kp = min(K, args.dyn_plain_steps)
     h = torch.full((n,), 0.5 * ny, dtype=torch.float64, device="cuda")
     dyn = Q.LangevinDynamics(n, 1)
-    dyn.step(h, p, f, drift[0], diff[0])
+    dyn.step(h, p, f16, drift[0], diff[0])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(Kp):
-        dyn.step(h, p, f, drift[k], diff[k])
+        dyn.step(h, p, f16, drift[k], diff[k])
     torch.cuda.synchronize()
     out["plain_fp64_per_step_launches"] = {"value": Kp / (time.perf_counter() - t0),
                                            "steps": Kp}
+    # CPU oracle: LangevinDynamics::step on all host cores, the same Philox
+    # increments drawn inside the step, on the same coefficients
+    of = O.BSplineField(None, float(n), float(ny), coef=f16.coefficients())
+    op = O.params(float(n), 1.0, 0.5, 1)
+    hc = np.full(n, 0.5 * ny)
+    work = (np.empty(n), np.empty(n))
+    kc = max(10, args.dyn_cpu_steps)
+    O.langevin_step_philox(hc, op, of, drift[0], diff[0], 1, 0, omp=True, work=work)
+    t0 = time.perf_counter()
+    for k in range(1, kc + 1):
+        O.langevin_step_philox(hc, op, of, drift[k], diff[k], 1, k, omp=True, work=work)
+    tc = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": kc / tc, "unit": "steps/s", "cores": O.omp_max_threads(),
+                           "kind": "port",
+                           "sample": "%d steps of the oracle's LangevinDynamics::step (gradient, "
+                                     "Philox increments, update; OpenMP) at L=65536 from the "
+                                     "flat line" % kc}
+    del of
     out["value"] = out["fp64"]["value"]
     return out
 
@@ -487,17 +612,23 @@ def run_depinning(args, Q, torch):
     unit variance), linear, Gamma = 1, flat start at Ly/2; dstep = 0.5 cell,
     max_advance = Ly, runaway = 2 Ly, root_tol 1e-10, sweep_tol 1e-8. Ramp f
     by f_step until a block fails, then bisect f to 1e-10 relative from the
-    last blocked line. FP64 and FP32-velocity forms; the plain host-driven
-    form is timed on one block for its sweep rate."""
+    last blocked line. Velocities in FP64 in the reference's 16-tap order
+    (the form whose f_c the tests pin to the oracle's), in FP64 on the
+    cell-polynomial store, and from the FP32 coefficients; the plain
+    host-driven form is timed on one block for its sweep rate."""
     n = ny = args.dep_size
-    store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
-    fld = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2, store=store)
+    fld = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2,
+                                    store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    fld_poly = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2,
+                                         store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY)
     rp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
                     runaway=2.0 * ny, max_sweeps=args.dep_max_sweeps)
     out = {"metric": "time to f_c (ramp + bisection to 1e-10)", "unit": "s",
            "workload": "L=%d, %dx%d field xi=4, linear, Gamma=1, f_step=%g" % (n, n, ny, args.dep_fstep)}
     crit = {}
-    for name, prec in (("fp64", Q.QEW_PREC_FP64), ("fp32split", Q.QEW_PREC_FP32_SPLIT)):
+    for name, prec in (("fp64", Q.QEW_PREC_FP64), ("fp64_poly", Q.QEW_PREC_FP64),
+                       ("fp32split", Q.QEW_PREC_FP32_SPLIT)):
+        fld_k = fld_poly if name == "fp64_poly" else fld
         h = torch.full((n,), 0.5 * ny, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -505,7 +636,7 @@ def run_depinning(args, Q, torch):
         k = 0
         while k * args.dep_fstep <= args.dep_fmax:
             fk = k * args.dep_fstep
-            r = Q.rk_block(h, Q.Params(float(n), 1.0, fk, Q.Model.Linear), fld, rp, precision=prec)
+            r = Q.rk_block(h, Q.Params(float(n), 1.0, fk, Q.Model.Linear), fld_k, rp, precision=prec)
             sweeps += r.sweeps
             blocks += 1
             log("  depinning %s f=%.3f blocked=%d sweeps=%d" % (name, fk, r.blocked, r.sweeps))
@@ -519,7 +650,7 @@ def run_depinning(args, Q, torch):
                ("runaway" if r.runaway else "max_sweeps")}
         if f_lo is not None and f_hi is not None:
             br = Q.depinning_bisect_report(h_lo, Q.Params(float(n), 1.0, 0.0, Q.Model.Linear),
-                                           fld, rp, f_lo, f_hi, rtol=1e-10, max_steps=64,
+                                           fld_k, rp, f_lo, f_hi, rtol=1e-10, max_steps=64,
                                            precision=prec)
             torch.cuda.synchronize()
             res.update({"f_c": br.f_c, "bracket": [br.f_lo, br.f_hi], "bisect_blocks": br.blocks,
@@ -533,6 +664,10 @@ def run_depinning(args, Q, torch):
             crit[name] = h_lo
         res["wall_s"] = time.perf_counter() - t0
         out[name] = res
+    if "fp64" in crit and "fp64_poly" in crit:
+        out["fp64_poly_vs_fp64"] = {
+            "f_c_rel_diff": abs(out["fp64_poly"]["f_c"] - out["fp64"]["f_c"]) / out["fp64"]["f_c"],
+            "max_abs_h_diff_critical": float((crit["fp64"] - crit["fp64_poly"]).abs().max())}
     if "fp64" in crit and "fp32split" in crit:
         out["fp32_vs_fp64"] = {
             "f_c_rel_diff": abs(out["fp32split"]["f_c"] - out["fp64"]["f_c"]) / out["fp64"]["f_c"],
@@ -540,17 +675,20 @@ def run_depinning(args, Q, torch):
         # sweep rate: resident vs plain host-driven, one block at the last blocked force
         p_lo = Q.Params(float(n), 1.0, out["fp64"]["f_lo"], Q.Model.Linear)
         rates = {}
-        for form in (Q.QEW_RK_RESIDENT, Q.QEW_RK_PLAIN):
+        for label, form, fk, prec in (
+                ("resident", Q.QEW_RK_RESIDENT, fld, Q.QEW_PREC_FP64),
+                ("resident_poly", Q.QEW_RK_RESIDENT, fld_poly, Q.QEW_PREC_FP64),
+                ("resident_reference_exact", Q.QEW_RK_RESIDENT, fld, Q.QEW_PREC_FP64_REFERENCE),
+                ("plain", Q.QEW_RK_PLAIN, fld, Q.QEW_PREC_FP64)):
             h = crit["fp64"].clone()
             rpp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
                              runaway=2.0 * ny, max_sweeps=args.dep_rate_sweeps)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            r = Q.rk_block(h, Q.Params(float(n), 1.0, out["fp64"]["f_c"], Q.Model.Linear), fld,
-                           rpp, form=form)
+            r = Q.rk_block(h, Q.Params(float(n), 1.0, out["fp64"]["f_c"], Q.Model.Linear), fk,
+                           rpp, form=form, precision=prec)
             torch.cuda.synchronize()
-            rates["resident" if form == Q.QEW_RK_RESIDENT else "plain"] = \
-                r.sweeps / (time.perf_counter() - t0)
+            rates[label] = r.sweeps / (time.perf_counter() - t0)
         out["sweeps_per_s"] = rates
     out["value"] = out["fp64"]["wall_s"]
     return out
@@ -697,8 +835,9 @@ def run_ours(args):
     # gradients of all n_inst lines:
     #   fp64            FP64 drop-in: the cell-polynomial store, one batched
     #                   persistent launch (k_gradient_poly)
-    #   fp64_reference  FP64 in the reference's 16-tap order, one launch per
-    #                   line (k_gradient)
+    #   fp64_reference  FP64 with the reference's arithmetic bit for bit (its
+    #                   16-tap order, true divisions, no fused multiply-adds),
+    #                   one launch per line (k_gradient)
     #   fp32split       FP32 split-index gather on the x-filtered FP32 store,
     #                   one batched persistent launch (k_gradient_split_persist)
     def step_fp64():
@@ -713,7 +852,8 @@ def run_ours(args):
     poly_kernel = "k_gradient" if args.no_poly_store else "k_gradient_poly"
     forms = {
         "fp64": (step_fp64, 48.0, poly_kernel, "f64"),
-        "fp64_reference": (step_fp64_ref, 48.0, "k_gradient", "f64"),
+        "fp64_reference": (step_fp64_ref, 48.0, "k_gradient (reference-exact arithmetic)",
+                           "f64"),
         "fp32split": (step_split, 28.0,
                       "k_gradient_split" if args.no_edge_store else "k_gradient_split_persist",
                       "f32"),
@@ -832,11 +972,15 @@ def run_ours(args):
         for name in (head,) + tuple(k for k in ("fp64", "fp32split") if k != head):
             results[name]["e2e"] = e2e_rate(name, e2e_prec[name])
         e2e = results[head]["e2e"]
-    static = ensemble = dynamics = depinning = serving = None
+    refshape = static = ensemble = dynamics = depinning = serving = None
     sections = set(s.strip() for s in args.sections.split(",") if s.strip())
     if not args.profile_run and sections:
         del noise, cells, fracs, g32, G, H
         torch.cuda.empty_cache()
+        if "refshape" in sections:
+            log("reference benchmark shape section")
+            refshape = run_reference_shape(args, Q, torch)
+            torch.cuda.empty_cache()
         if "static" in sections:
             log("static section")
             static = run_static(args, Q, torch)
@@ -874,7 +1018,8 @@ def run_ours(args):
                 "roofline": head_r["roofline"], "fp64_roofline": head_r["fp64_roofline"],
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "forms": {k: v for k, v in results.items() if k != head},
-                "static": static, "ensemble": ensemble, "dynamics": dynamics,
+                "reference_shape": refshape, "static": static, "ensemble": ensemble,
+                "dynamics": dynamics,
                 "depinning": depinning, "serving": serving}
         print(json.dumps(line), flush=True)
     if ws > 1:

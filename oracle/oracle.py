@@ -106,6 +106,9 @@ def lib():
                                              C.POINTER(C.c_long)]
         L.qo_depinning_bisect_ex.restype = I
         L.qo_philox_normals.argtypes = [C.c_uint64, C.c_uint64, I, PD]
+        L.qo_langevin_step_philox.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise), D,
+                                              D, C.c_uint64, C.c_uint64, PD, PD, I]
+        L.qo_omp_set_threads.argtypes = [I]
         L.qo_fire_minimize.argtypes = [PD, I, C.POINTER(QoParams), C.POINTER(QoNoise),
                                        C.POINTER(QoFireParams), C.POINTER(QoFireResult)]
         L.qo_mt64_seed.argtypes = [C.c_void_p, C.c_uint64]
@@ -135,10 +138,15 @@ class Noise:
 class BSplineField(Noise):
     """FilteredNoise(field, nx, ny, Lx, Ly), filtered_noise.cpp:84-90."""
 
-    def __init__(self, field_xy: np.ndarray, Lx: float, Ly: float,
+    def __init__(self, field_xy: np.ndarray | None, Lx: float, Ly: float,
                  coef: np.ndarray | None = None):
-        field_xy = np.ascontiguousarray(field_xy, dtype=np.float64)
-        nx, ny = field_xy.shape
+        """field_xy may be None when the prefiltered coefficients are given."""
+        if field_xy is None:
+            field_xy = np.empty((0, 0))
+            nx, ny = np.shape(coef)
+        else:
+            field_xy = np.ascontiguousarray(field_xy, dtype=np.float64)
+            nx, ny = field_xy.shape
         super().__init__(0)
         if coef is None:
             coef = prefilter(field_xy)
@@ -247,6 +255,20 @@ def langevin_step(h: np.ndarray, p: QoParams, noise: Noise, drift, diff, xi):
     xi = np.ascontiguousarray(xi, dtype=np.float64)
     g = np.empty_like(h)
     lib().qo_langevin_step(_p(h), h.size, C.byref(p), C.byref(noise.s), drift, diff, _p(xi), _p(g))
+
+
+def langevin_step_philox(h: np.ndarray, p: QoParams, noise: Noise, drift, diff, seed, step,
+                         omp=False, work=None):
+    """LangevinDynamics::step with the Philox normals of (seed, step) drawn in
+    the step (the increments the GPU's step uses); omp=True on all threads."""
+    g, xi = work if work is not None else (np.empty_like(h), np.empty_like(h))
+    lib().qo_langevin_step_philox(_p(h), h.size, C.byref(p), C.byref(noise.s), drift, diff,
+                                  seed, step, _p(g), _p(xi), 1 if omp else 0)
+
+
+def set_threads(k: int) -> None:
+    """OpenMP threads of the oracle's parallel forms."""
+    lib().qo_omp_set_threads(int(k))
 
 
 def rk_params(dstep=0.0, max_advance=0.0, root_tol=1e-10, sweep_tol=1e-9,

@@ -1090,9 +1090,10 @@ static void philox4x32_10(uint32_t c[4], uint64_t seed) {
 /* Increment i of step `step`: block j = i/2 of counter (j, step) gives two
  * 53-bit uniforms u1 in (0,1], u2 in [0,1); Box-Muller
  * r = sqrt(-2 ln u1), z0 = r cos(2 pi u2), z1 = r sin(2 pi u2). */
-void qo_philox_normals(uint64_t seed, uint64_t step, int n, double *out) {
+static void philox_normals_impl(uint64_t seed, uint64_t step, int n, double *out, int par) {
     const double two_pi = 6.283185307179586476925286766559;
-    for (int j = 0; 2 * j < n; ++j) {
+#pragma omp parallel for schedule(static) if (par)
+    for (int j = 0; j < (n + 1) / 2; ++j) {
         uint32_t c[4] = {(uint32_t)j, 0u, (uint32_t)step, (uint32_t)(step >> 32)};
         philox4x32_10(c, seed);
         const uint64_t a = (((uint64_t)c[0] << 32) | c[1]) >> 11;
@@ -1104,4 +1105,35 @@ void qo_philox_normals(uint64_t seed, uint64_t step, int n, double *out) {
         out[2 * j] = r * cos(ang);
         if (2 * j + 1 < n) out[2 * j + 1] = r * sin(ang);
     }
+}
+
+void qo_philox_normals(uint64_t seed, uint64_t step, int n, double *out) {
+    philox_normals_impl(seed, step, n, out, 0);
+}
+
+/* LangevinDynamics::step (dynamics.h:34-64) with its own increments: the
+ * Philox normals of (seed, step) drawn inside the step, as the reference
+ * draws from its generator pool; par = 1 runs the gradient, the draws and
+ * the update on all OpenMP threads (the timed CPU form). */
+void qo_langevin_step_philox(double *h, int n, const qo_params *p, const qo_noise *nz,
+                             double drift, double diff, uint64_t seed, uint64_t step,
+                             double *grad, double *xi, int par) {
+    qo_gradient_impl(h, n, p, nz, grad, par);
+    const double a = drift, b = diff;
+    if (b > 0) {
+        philox_normals_impl(seed, step, n, xi, par);
+#pragma omp parallel for schedule(static) if (par)
+        for (int i = 0; i < n; ++i) h[i] += -a * grad[i] + b * xi[i];
+    } else {
+#pragma omp parallel for schedule(static) if (par)
+        for (int i = 0; i < n; ++i) h[i] += -a * grad[i];
+    }
+}
+
+void qo_omp_set_threads(int k) {
+#ifdef _OPENMP
+    omp_set_num_threads(k > 0 ? k : 1);
+#else
+    (void)k;
+#endif
 }

@@ -178,6 +178,10 @@ int qo_depinning_bisect_ex(double *h, int n, const qo_params *p,
 /* ---- Philox4x32-10 counter RNG + Box-Muller normals (shared with the GPU
  * Langevin step, so the oracle can regenerate the same increments) ---- */
 void qo_philox_normals(uint64_t seed, uint64_t step, int n, double *out);
+void qo_langevin_step_philox(double *h, int n, const qo_params *p, const qo_noise *nz,
+                             double drift, double diff, uint64_t seed, uint64_t step,
+                             double *grad, double *xi, int par);
+void qo_omp_set_threads(int k);
 
 #ifdef __cplusplus
 }

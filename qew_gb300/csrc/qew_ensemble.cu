@@ -27,6 +27,8 @@ constexpr int kEnsBS = 512;
 
 struct EnsJob {
     const double *coef64;
+    const double *poly64;  // FP64 cell-polynomial store, or null
+    int ky;                // y * 2^ky == y / dy, or kPolyNotPow2
     const float *coef32;
     const float *edge32;
     int nx, ny;
@@ -53,6 +55,8 @@ __device__ __forceinline__ NoiseBSpline64 job_noise64(const EnsJob &j) {
     nz.wxc[1] = 2.875 * (1.0 / 6.0);
     nz.wxc[2] = 2.875 * (1.0 / 6.0);
     nz.wxc[3] = 0.125 * (1.0 / 6.0);
+    nz.poly = (j.n == j.nx && j.p.physical_size == j.Lx) ? j.poly64 : nullptr;
+    nz.ky = j.ky;
     return nz;
 }
 
@@ -127,6 +131,8 @@ extern "C" qew_status qew_ensemble_minimize(qew_ctx *ctx, int count, const qew_e
                             "coefficients", k, use32 ? " and FP32" : "");
         EnsJob &j = jobs[k];
         j.coef64 = f->coef64;
+        j.poly64 = f->poly64;
+        j.ky = make_bspline64(f).ky;
         j.coef32 = f->coef32;
         j.edge32 = f->edge32;
         j.nx = f->nx;

@@ -170,6 +170,73 @@ __host__ __device__ __forceinline__ LineDx make_line_dx(double physical_size, in
     return L;
 }
 
+// ------------------------------------------ FP64 cell-polynomial store
+// (QEW_STORE_FP64_POLY): per (row cell j, column e) the cubic of the
+// x-filtered field at x = e + 1/2 in the row fraction t, as
+// {q0, q1, q2, v0} with dV/dy = q0 + t (q1 + t q2) and
+// V = v0 + dy t (q0 + t (q1/2 + t q2/3)); qew_poly.cuh derives it.
+// Marker for a row spacing that is not a power of two.
+constexpr int kPolyNotPow2 = 1 << 20;
+
+// 256-bit read-only load of one cell {q0, q1, q2, v0} (32-byte aligned).
+__device__ __forceinline__ void poly_load4(const double *p, double &q0, double &q1, double &q2,
+                                           double &v0) {
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
+        : "=d"(q0), "=d"(q1), "=d"(q2), "=d"(v0)
+        : "l"(p));
+}
+__device__ __forceinline__ void poly_load3(const double *p, double &q0, double &q1, double &q2) {
+    double v0;
+    poly_load4(p, q0, q1, q2, v0);
+}
+
+// g = a * 2^k. When g is finite, normal and in [0, ny) (ny < 2^30): iy =
+// floor(g), t = g - iy exactly, and true; otherwise false (negative, >= ny,
+// non-finite or subnormal heights take the reference's fold instead). Only
+// integer operations on the bits of a.
+__device__ __forceinline__ bool poly_cell_exact(double a, int k, int ny, int &iy, double &t) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+    const int ef = (int)(b >> 52);  // sign bit and biased exponent
+    if (ef == 0) {                  // +0 (or a subnormal: the slow path)
+        iy = 0;
+        t = 0.0;
+        return b == 0ull;
+    }
+    if (ef >= 2047) return false;   // negative, infinite or NaN
+    const int eb = ef + k;          // biased exponent of g
+    if (eb <= 0) return false;
+    const int e = eb - 1023;
+    if (e < 0) {                    // g in (0, 1): cell 0, t = g
+        iy = 0;
+        t = __longlong_as_double((long long)(b + ((unsigned long long)(long long)k << 52)));
+        return true;
+    }
+    if (e > 29) return false;
+    const unsigned long long m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+    const int sh = 52 - e;          // 23 .. 52 fraction bits
+    iy = (int)(m >> sh);
+    if (iy >= ny) return false;
+    const unsigned long long fb = m & ((1ull << sh) - 1ull);
+    if (fb == 0ull) {
+        t = 0.0;
+        return true;
+    }
+    const int top = 63 - __clzll((long long)fb);  // leading bit of the fraction, < sh
+    const unsigned long long mant = (fb << (52 - top)) & 0x000FFFFFFFFFFFFFull;
+    t = __longlong_as_double((long long)(((unsigned long long)(top - sh + 1023) << 52) | mant));
+    return true;
+}
+
+// dV/dy and V of a cell at fraction t.
+__device__ __forceinline__ double poly_dvdy(double q0, double q1, double q2, double t) {
+    return fma(fma(q2, t, q1), t, q0);
+}
+__device__ __forceinline__ double poly_value(double q0, double q1, double q2, double v0, double t,
+                                             double dy) {
+    const double third = 1.0 / 3.0;
+    return fma(dy * t, fma(fma(q2 * third, t, 0.5 * q1), t, q0), v0);
+}
+
 // DeviceNoise on x-fastest FP64 coefficients.
 struct NoiseBSpline64 {
     const double *__restrict__ coef;  // [ny][nx]
@@ -182,6 +249,19 @@ struct NoiseBSpline64 {
     // of t = 1/2 (bit-identical to locating it).
     bool xconst;
     double wxc[4];
+    // The field's FP64 cell-polynomial store when it serves this line (one
+    // point per field column), else null; ky: y * 2^ky == y / dy exactly
+    // (kPolyNotPow2 when dy is not a power of two).
+    const double *__restrict__ poly;
+    int ky;
+
+    // Row cell and fraction of height y: from y's bits when dy is a power of
+    // two and y / dy lies in [0, ny), else the reference's locate.
+    __device__ __forceinline__ void poly_row(double y, int &iy, double &t) const {
+        const bool ok = (ky != kPolyNotPow2) ? poly_cell_exact(y, ky, ny, iy, t)
+                                              : poly_cell_exact(y * inv_dy, 0, ny, iy, t);
+        if (!ok) grid_locate(y, dy, inv_dy, dy_pow2, ny, iy, t);
+    }
 
     __device__ __forceinline__ double c(int ix, int iy) const {
         return __ldg(coef + (size_t)iy * (size_t)nx + ix);
@@ -229,8 +309,17 @@ struct NoiseBSpline64 {
         }
         return dy_pow2 ? dg * inv_dy : dg / dy;
     }
-    // dV/dy / V at the midpoint of edge e (xc its physical x).
+    // dV/dy / V at the midpoint of edge e (xc its physical x). With the
+    // cell-polynomial store: one 32-byte cell and two FMAs (the wrap edge,
+    // e = nx - 1, is not at a half-integer column and keeps the 16 taps).
     __device__ __forceinline__ double dvdy_edge(int e, double xc, double y) const {
+        if (poly && e + 1 < nx) {
+            int iy;
+            double t, q0, q1, q2;
+            poly_row(y, iy, t);
+            poly_load3(poly + ((size_t)iy * (size_t)nx + (size_t)e) * 4, q0, q1, q2);
+            return poly_dvdy(q0, q1, q2, t);
+        }
         if (!xconst || e + 1 >= nx) return dvdy(xc, y);
         int iy, xs[4], iyn[4];
         double fy, dwy[4];
@@ -249,6 +338,13 @@ struct NoiseBSpline64 {
         return dy_pow2 ? dg * inv_dy : dg / dy;
     }
     __device__ __forceinline__ double value_edge(int e, double xc, double y) const {
+        if (poly && e + 1 < nx) {
+            int iy;
+            double t, q0, q1, q2, v0;
+            poly_row(y, iy, t);
+            poly_load4(poly + ((size_t)iy * (size_t)nx + (size_t)e) * 4, q0, q1, q2, v0);
+            return poly_value(q0, q1, q2, v0, t, dy);
+        }
         if (!xconst || e + 1 >= nx) return value(xc, y);
         int iy, xs[4], iyn[4];
         double fy, wy[4];
@@ -507,6 +603,14 @@ static inline NoiseBSpline64 make_bspline64(const qew_field *f, int n = 0,
     nz.inv_dy = 1.0 / f->dy;
     nz.dx_pow2 = qew_is_pow2(f->dx);
     nz.dy_pow2 = qew_is_pow2(f->dy);
+    nz.poly = (f->poly64 && f->coef64 && n > 0 && n == f->nx && physical_size == f->Lx)
+                  ? f->poly64
+                  : nullptr;
+    {
+        int e;
+        const double m = frexp(f->dy, &e);  // dy = m 2^e
+        nz.ky = (f->dy > 0 && m == 0.5) ? 1 - e : kPolyNotPow2;
+    }
     return nz;
 }
 

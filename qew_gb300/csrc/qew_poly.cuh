@@ -27,58 +27,6 @@
 
 #include "qew_internal.cuh"
 
-// Marker for a row spacing that is not a power of two.
-constexpr int kPolyNotPow2 = 1 << 20;
-
-// 256-bit read-only load of one cell {q0, q1, q2, v0} (32-byte aligned).
-__device__ __forceinline__ void poly_load4(const double *p, double &q0, double &q1, double &q2,
-                                           double &v0) {
-    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];"
-        : "=d"(q0), "=d"(q1), "=d"(q2), "=d"(v0)
-        : "l"(p));
-}
-__device__ __forceinline__ void poly_load3(const double *p, double &q0, double &q1, double &q2) {
-    double v0;
-    poly_load4(p, q0, q1, q2, v0);
-}
-
-// g = a * 2^k. When g is finite, normal and in [0, ny) (ny < 2^30): iy =
-// floor(g), t = g - iy exactly, and true; otherwise false (negative, >= ny,
-// non-finite or subnormal heights take the reference's fold instead). Only
-// integer operations on the bits of a.
-__device__ __forceinline__ bool poly_cell_exact(double a, int k, int ny, int &iy, double &t) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(a);
-    const int ef = (int)(b >> 52);  // sign bit and biased exponent
-    if (ef == 0) {                  // +0 (or a subnormal: the slow path)
-        iy = 0;
-        t = 0.0;
-        return b == 0ull;
-    }
-    if (ef >= 2047) return false;   // negative, infinite or NaN
-    const int eb = ef + k;          // biased exponent of g
-    if (eb <= 0) return false;
-    const int e = eb - 1023;
-    if (e < 0) {                    // g in (0, 1): cell 0, t = g
-        iy = 0;
-        t = __longlong_as_double((long long)(b + ((unsigned long long)(long long)k << 52)));
-        return true;
-    }
-    if (e > 29) return false;
-    const unsigned long long m = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
-    const int sh = 52 - e;          // 23 .. 52 fraction bits
-    iy = (int)(m >> sh);
-    if (iy >= ny) return false;
-    const unsigned long long fb = m & ((1ull << sh) - 1ull);
-    if (fb == 0ull) {
-        t = 0.0;
-        return true;
-    }
-    const int top = 63 - __clzll((long long)fb);  // leading bit of the fraction, < sh
-    const unsigned long long mant = (fb << (52 - top)) & 0x000FFFFFFFFFFFFFull;
-    t = __longlong_as_double((long long)(((unsigned long long)(top - sh + 1023) << 52) | mant));
-    return true;
-}
-
 // Row cell and fraction of the midpoint of edge heights (he, hep), given
 // a = he + hep: the exact bit path when it applies, else the reference's
 // locate (filtered_noise.h:80-92) on hc = a / 2.
@@ -87,16 +35,6 @@ __device__ __forceinline__ void poly_locate(double a, int ky, double half_inv_dy
     const bool ok = (ky != kPolyNotPow2) ? poly_cell_exact(a, ky, nz.ny, iy, t)
                                           : poly_cell_exact(a * half_inv_dy, 0, nz.ny, iy, t);
     if (!ok) grid_locate(a * 0.5, nz.dy, nz.inv_dy, nz.dy_pow2, nz.ny, iy, t);
-}
-
-// dV/dy and V of a cell at fraction t.
-__device__ __forceinline__ double poly_dvdy(double q0, double q1, double q2, double t) {
-    return fma(fma(q2, t, q1), t, q0);
-}
-__device__ __forceinline__ double poly_value(double q0, double q1, double q2, double v0, double t,
-                                             double dy) {
-    const double third = 1.0 / 3.0;
-    return fma(dy * t, fma(fma(q2 * third, t, 0.5 * q1), t, q0), v0);
 }
 
 // Scale exponent k with (h_e + h_ep) * 2^k == ((h_e + h_ep) / 2) / dy exactly,

@@ -39,8 +39,8 @@ __device__ __forceinline__ double rk_site_velocity(const Noise &nz, int i, int n
     const double hcl = (hl + hi) * 0.5;
     const double xcr = (double)(i + ip) * 0.5 * dx;
     const double hcr = (hi + hr) * 0.5;
-    const double dvl = nz.dvdy(xcl, hcl);
-    const double dvr = nz.dvdy(xcr, hcr);
+    const double dvl = noise_dvdy_edge(nz, im, xcl, hcl);  // edge (im, i)
+    const double dvr = noise_dvdy_edge(nz, i, xcr, hcr);   // edge (i, ip)
     const double grad = dx * (line_force + 0.5 * (dvl + dvr) - f);
     return -grad;
 }
@@ -217,7 +217,7 @@ __device__ __forceinline__ double rk_site_velocity_pair(const Noise &nz, int i, 
     }
     const double xc = lane ? (double)(i + ip) * 0.5 * dx : (double)(im + i) * 0.5 * dx;
     const double hc = lane ? (hi + hr) * 0.5 : (hl + hi) * 0.5;
-    const double mine = nz.dvdy(xc, hc);
+    const double mine = noise_dvdy_edge(nz, lane ? i : im, xc, hc);
     const double other = __shfl_xor_sync(pmask, mine, 1);
     const double dvl = lane ? other : mine;
     const double dvr = lane ? mine : other;

@@ -81,7 +81,7 @@ def test_cluster_matches_oracle(Q, O):
                           O.lbfgs_default_params(ftol=1e-7, precondition=1, precond_shift=0.1,
                                                  ls_fallback=1))
     assert r.converged and rc.converged
-    assert np.max(np.abs(npy(h) - hc)) < 1e-5
+    assert np.max(np.abs(npy(h) - hc)) < 2e-7  # 4.2e-8 measured (168 vs 156 iterations)
     e = Q.objective(h, Q.Params(Lx, 2.0, 0.0, Q.Model.Linear), f)
     ec = O.objective(hc, O.params(Lx, 2.0, 0.0, 0), of)
     assert abs(e - ec) <= 1e-11 * abs(ec)

@@ -76,11 +76,17 @@ def test_trajectory_matches_oracle(Q, O, form, model, precondition):
                           O.lbfgs_default_params(m=10, ftol=1e-7, max_iter=5000,
                                                  precondition=precondition))
     assert r.converged and ro.converged
-    # Over hundreds of iterations the GPU's tree reductions and the oracle's
-    # serial sums take different rounding-level Armijo decisions, so the
-    # iteration counts drift; both must reach the same minimiser.
-    assert abs(r.iterations - ro.iterations) <= max(5, ro.iterations // 4)
-    assert np.max(np.abs(npy(h) - ho)) < 1e-6
+    if precondition:
+        # a few well-conditioned iterations: the oracle's trajectory
+        assert (r.iterations, r.n_func_evals) == (ro.iterations, ro.n_func_evals)
+        assert np.max(np.abs(npy(h) - ho)) < 1e-12
+    else:
+        # Unpreconditioned (hundreds of iterations near an ill-conditioned
+        # minimum) the GPU's tree reductions and the oracle's serial sums take
+        # different rounding-level Armijo decisions: the counts drift (up to
+        # 12% measured on GB300) and both reach the same minimiser.
+        assert abs(r.iterations - ro.iterations) <= max(5, ro.iterations * 3 // 20)
+        assert np.max(np.abs(npy(h) - ho)) < 5e-7
     e_q = Q.objective(h, Q.Params(Lx, lt, 0.05, Q.Model(model)), f)
     e_o = O.objective(ho, O.params(Lx, lt, 0.05, model), of)
     assert abs(e_q - e_o) <= 1e-10 * abs(e_o)

@@ -170,3 +170,62 @@ def test_host_batch_mapped_and_copied_agree(Q):
             one = torch.empty(nx, dtype=torch.float64).pin_memory().numpy()
             Q.gradient_host(h[2].copy(), p, f, one, precision=prec)
             assert np.array_equal(one, dev[2])
+
+
+def test_poly_objective_and_solvers_match_oracle(Q, O):
+    """The store serves every FP64 consumer of the field on such a line: the
+    energy (the polynomial's value), the site velocities of the Rosso-Krauth
+    construction, a Langevin step with given increments and a preconditioned
+    L-BFGS solve agree with the oracle's reference-order arithmetic."""
+    nx, ny = 1024, 64
+    fld = gaussian_field(nx, ny, 4.0, 31)
+    f = poly_field(Q, fld, float(nx), float(ny))
+    of = O.BSplineField(fld, float(nx), float(ny), coef=f.coefficients())
+    rng = np.random.default_rng(4)
+    h = ny / 2 + np.cumsum(rng.standard_normal(nx)) * 0.2
+    h -= np.linspace(0, h[-1] - h[0], nx)
+    for model in (0, 1):
+        p = Q.Params(float(nx), 1.2, 0.15, Q.Model(model))
+        po = O.params(float(nx), 1.2, 0.15, model)
+        e, eo = Q.objective(t64(h), p, f), O.objective(h, po, of)
+        assert abs(e - eo) <= 1e-12 * abs(eo)
+        v = npy(Q.rk_site_velocity(t64(h), p, f))
+        close(v, -O.gradient(h, po, of))
+        xi = rng.standard_normal(nx)
+        hl = t64(h)
+        Q.LangevinDynamics(nx, 1).step_with_increments(hl, p, f, 0.01, 0.05, t64(xi))
+        ho = h.copy()
+        O.langevin_step(ho, po, of, 0.01, 0.05, xi)
+        close(npy(hl), ho)
+    p = Q.Params(float(nx), 1.0, 0.0, Q.Model.Linear)
+    lp = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=2000, precondition=True, precond_shift=0.03)
+    hg = t64(np.full(nx, ny / 2))
+    r = Q.lbfgs_minimize(hg, p, f, lp)
+    ho = np.full(nx, ny / 2)
+    ro = O.lbfgs_minimize(ho, O.params(float(nx), 1.0, 0.0, 0), of,
+                          O.lbfgs_default_params(m=10, ftol=1e-8, max_iter=2000, precondition=1,
+                                                 precond_shift=0.03))
+    assert r.converged and ro.converged
+    assert np.max(np.abs(npy(hg) - ho)) < 1e-7
+    e, eo = Q.objective(hg, p, f), O.objective(ho, O.params(float(nx), 1.0, 0.0, 0), of)
+    assert abs(e - eo) <= 1e-12 * abs(eo)
+
+
+def test_poly_rk_block_close_to_reference_order(Q, O):
+    """Rosso-Krauth sweeps on the store: the oracle's verdict, the sweep count
+    within one, lines within rounding-level distances."""
+    n, ny = 512, 64
+    fld = gaussian_field(n, ny, 4.0, 41)
+    f = poly_field(Q, fld, float(n), float(ny))
+    of = O.BSplineField(fld, float(n), float(ny), coef=f.coefficients())
+    rp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
+                    runaway=2.0 * ny, max_sweeps=3000)
+    orp = O.rk_params(0.5, float(ny), 1e-10, 1e-8, 2.0 * ny, 3000)
+    for fdr in (0.0, 0.05):
+        hg = t64(np.full(n, ny / 2))
+        r = Q.rk_block(hg, Q.Params(float(n), 1.0, fdr, Q.Model.Linear), f, rp)
+        ho = np.full(n, ny / 2)
+        ro = O.rk_block(ho, O.params(float(n), 1.0, fdr, 0), of, orp)
+        assert (r.blocked, r.runaway) == (bool(ro.blocked), bool(ro.runaway))
+        assert abs(r.sweeps - ro.sweeps) <= 1
+        assert np.max(np.abs(npy(hg) - ho)) < 1e-8

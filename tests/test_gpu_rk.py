@@ -50,8 +50,14 @@ def test_rk_block_matches_oracle(Q, O, model):
         ro = O.rk_block(ho, O.params(Lx, 1.0, fdr, model), of,
                         O.rk_params(0.5 / ny, Ly, 1e-11, 1e-9, 3 * Ly))
         assert r.blocked == bool(ro.blocked) and r.runaway == bool(ro.runaway)
-        assert abs(r.sweeps - ro.sweeps) <= 2
-        assert np.max(np.abs(npy(h) - ho)) < 1e-9
+        assert r.sweeps == ro.sweeps
+        assert np.max(np.abs(npy(h) - ho)) < 1e-12
+        # the reference-exact arithmetic: the oracle's line bit for bit
+        he = t64(np.full(nx, 0.5))
+        re = Q.rk_block(he, Q.Params(Lx, 1.0, fdr, Q.Model(model)), f,
+                        rkp(Q, 0.5 / ny, Ly, 1e-11, 1e-9, 3 * Ly),
+                        precision=Q.QEW_PREC_FP64_REFERENCE)
+        assert re.sweeps == ro.sweeps and np.array_equal(npy(he), ho)
 
 
 def test_blocked_is_forward_and_arrested(Q):
