@@ -198,13 +198,14 @@ def test_poly_objective_and_solvers_match_oracle(Q, O):
         O.langevin_step(ho, po, of, 0.01, 0.05, xi)
         close(npy(hl), ho)
     p = Q.Params(float(nx), 1.0, 0.0, Q.Model.Linear)
-    lp = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=2000, precondition=True, precond_shift=0.03)
+    lp = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=2000, precondition=True, precond_shift=0.03,
+                       ls_fallback=True)
     hg = t64(np.full(nx, ny / 2))
     r = Q.lbfgs_minimize(hg, p, f, lp)
     ho = np.full(nx, ny / 2)
     ro = O.lbfgs_minimize(ho, O.params(float(nx), 1.0, 0.0, 0), of,
                           O.lbfgs_default_params(m=10, ftol=1e-8, max_iter=2000, precondition=1,
-                                                 precond_shift=0.03))
+                                                 precond_shift=0.03, ls_fallback=1))
     assert r.converged and ro.converged
     assert np.max(np.abs(npy(hg) - ho)) < 1e-7
     e, eo = Q.objective(hg, p, f), O.objective(ho, O.params(float(nx), 1.0, 0.0, 0), of)
