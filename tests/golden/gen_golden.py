@@ -14,13 +14,13 @@ with numpy/scipy and writes the arrays as ``.npz``:
   SciPy's fmin_l_bfgs_b on the reference energy (reference
   gen_lbfgs_golden.py:21-70).
 
-When the reference tree is present (``--reference DIR``, default the mounted
-copy) the script also checks that the regenerated arrays occur byte-for-byte
+When the reference source tree is given (``--reference DIR``, or the
+environment variable QEW_REFERENCE_TREE) the script also checks that the regenerated arrays occur byte-for-byte
 in the reference's committed ``.h5`` files, and reads the committed ``e_min``
 attribute (a little-endian double at byte offset 1192 of lbfgs_golden.h5) so
 the fixture carries the reference's own number next to the recomputed one.
 
-Run:  python tests/golden/gen_golden.py
+Run:  python tests/golden/gen_golden.py --reference <reference source tree>
 """
 from __future__ import annotations
 
@@ -121,11 +121,13 @@ def check_against_reference(ref_dir, ng, lg):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("QEW_REFERENCE_TREE", ""),
+                    help="the reference's source tree (its tests/data/*.h5 are checked)")
     args = ap.parse_args()
     ng = noise_golden()
     lg = lbfgs_golden()
-    chk = check_against_reference(args.reference, ng, lg) if os.path.isdir(args.reference) else {}
+    have_ref = bool(args.reference) and os.path.isdir(args.reference)
+    chk = check_against_reference(args.reference, ng, lg) if have_ref else {}
     print("reference cross-check:", chk if chk else "reference tree not present")
     e_ref = chk.get("lbfgs_e_min_ref", np.nan)
     verified = bool(chk) and all(v for k, v in chk.items() if k != "lbfgs_e_min_ref")
