@@ -680,9 +680,15 @@ def run_depinning(args, Q, torch):
                 ("resident_poly", Q.QEW_RK_RESIDENT, fld_poly, Q.QEW_PREC_FP64),
                 ("resident_reference_exact", Q.QEW_RK_RESIDENT, fld, Q.QEW_PREC_FP64_REFERENCE),
                 ("plain", Q.QEW_RK_PLAIN, fld, Q.QEW_PREC_FP64)):
-            h = crit["fp64"].clone()
             rpp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
                              runaway=2.0 * ny, max_sweeps=args.dep_rate_sweeps)
+            # one untimed block first: a class's first call runs the autotuner's probe
+            Q.rk_block(crit["fp64"].clone(),
+                       Q.Params(float(n), 1.0, out["fp64"]["f_c"], Q.Model.Linear), fk,
+                       Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10,
+                                  sweep_tol=1e-8, runaway=2.0 * ny, max_sweeps=32),
+                       form=form, precision=prec)
+            h = crit["fp64"].clone()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             r = Q.rk_block(h, Q.Params(float(n), 1.0, out["fp64"]["f_c"], Q.Model.Linear), fk,
@@ -1018,6 +1024,7 @@ def run_ours(args):
                 "roofline": head_r["roofline"], "fp64_roofline": head_r["fp64_roofline"],
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "forms": {k: v for k, v in results.items() if k != head},
+                "autotune": [ln for ln in Q.tune_report().splitlines() if ln],
                 "reference_shape": refshape, "static": static, "ensemble": ensemble,
                 "dynamics": dynamics,
                 "depinning": depinning, "serving": serving}

@@ -575,6 +575,33 @@ qew_status qew_depinning_bisect_ex(qew_ctx *ctx, const qew_field *field,
                                    int precision, qew_bisect_result *res,
                                    int *h_verdicts);
 
+/* ------------------------------------------------------------- autotuner */
+/* Launch shapes chosen by measurement (no reference counterpart). Kernels
+ * with several launch shapes that give bitwise-identical results time every
+ * candidate on the first call of a (device, kernel, shape class) -- the
+ * call's own work, CUDA events on the context's stream -- and keep the
+ * fastest for the rest of the process:
+ *   0 QEW_TUNE_GRADIENT_POLY   FP64 store gather: sites per thread {1,2,4} x
+ *                              resident CTAs per SM {2,3,4} (9 candidates)
+ *   1 QEW_TUNE_GRADIENT_SPLIT  FP32 split gather on the x-filtered store: sites
+ *                              per thread {1,2} x CTAs per SM {4,6,8} (6)
+ *   2 QEW_TUNE_RK_SEARCH       Rosso-Krauth forward-zero search: 8-lane groups,
+ *                              lane pairs, one lane (3; timed for 8 sweeps on
+ *                              a copy of the line advanced 24 sweeps; replaces
+ *                              the warps-budget default only when more than
+ *                              20 % faster)
+ * The shape class is the log2 of the work (points) and the kernel's variant
+ * (model; noise form and GPU share for the sweeps). */
+enum { QEW_TUNE_GRADIENT_POLY = 0, QEW_TUNE_GRADIENT_SPLIT = 1, QEW_TUNE_RK_SEARCH = 2 };
+/* on = 0: this context uses the hand-chosen default shapes. */
+qew_status qew_ctx_set_autotune(qew_ctx *ctx, int on);
+/* Fixes kernel's candidate for this context (-1: tuned or default again). */
+qew_status qew_ctx_force_tune_candidate(qew_ctx *ctx, int kernel, int candidate);
+/* The tuned choices of this process, one line per (device, kernel, class)
+ * with every candidate's time; writes at most size-1 characters and a NUL,
+ * returns the full length. */
+int qew_tune_report(char *buf, int size);
+
 /* ------------------------------------------------------------ measurement */
 /* FP64 FMA instructions per second of this GPU (no reference counterpart: the
  * roof of the FP64-pipe-bound gather). Eight resident CTAs per SM, each

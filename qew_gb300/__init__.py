@@ -41,6 +41,7 @@ from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # n
                     QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT, QEW_PREC_FP32_SPLIT,
                     QEW_PREC_FP64, QEW_PREC_FP64_REFERENCE, QEW_RK_PLAIN, QEW_RK_RESIDENT,
                     QEW_STORE_FP32, QEW_STORE_FP32_EDGE, QEW_STORE_FP64, QEW_STORE_FP64_POLY,
+                    QEW_TUNE_GRADIENT_POLY, QEW_TUNE_GRADIENT_SPLIT, QEW_TUNE_RK_SEARCH,
                     QewError)
 
 __all__ = [
@@ -54,6 +55,7 @@ __all__ = [
     "StaticConfig", "StaticProfile", "static_sweep", "DynamicConfig", "DynamicSnapshot",
     "DynamicResult", "dynamic_anneal", "DepinningConfig", "DepinningStep", "DepinningResult",
     "depinning_ramp", "FireParams", "FireResult", "fire_minimize", "line_statistics",
+    "tune_report",
 ]
 
 
@@ -162,6 +164,15 @@ class Context:
         _capi.check(self.lib.qew_ctx_set_barrier_limits(self.h, int(max_polls), int(skip_block)),
                     self.h, "set_barrier_limits")
 
+    def set_autotune(self, on: bool = True):
+        """Launch shapes by measurement (True) or the hand-chosen defaults."""
+        _capi.check(self.lib.qew_ctx_set_autotune(self.h, int(bool(on))), self.h, "autotune")
+
+    def force_tune_candidate(self, kernel: int, candidate: int = -1):
+        """Fix one tuned kernel's launch shape for this context (-1: release)."""
+        _capi.check(self.lib.qew_ctx_force_tune_candidate(self.h, int(kernel), int(candidate)),
+                    self.h, "force_tune_candidate")
+
     def measure_fp64_fma_rate(self, iters: int = 4096):
         """(FP64 FMA instructions per second, timed ms) of this GPU."""
         self.sync_stream()
@@ -178,6 +189,15 @@ class Context:
                 self.h = None
         except Exception:
             pass
+
+
+def tune_report() -> str:
+    """The autotuner's choices in this process (qew_tune_report)."""
+    lib = _capi.load()
+    n = lib.qew_tune_report(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    lib.qew_tune_report(buf, n + 1)
+    return buf.value.decode()
 
 
 _contexts: dict[int, Context] = {}

@@ -32,6 +32,7 @@ QEW_PREC_FP64, QEW_PREC_FP32_SPLIT, QEW_PREC_FP64_REFERENCE = 0, 1, 2
 QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
 QEW_NOALLOC_MAX_N = 1048576
 QEW_RK_PLAIN, QEW_RK_RESIDENT = 0, 1
+QEW_TUNE_GRADIENT_POLY, QEW_TUNE_GRADIENT_SPLIT, QEW_TUNE_RK_SEARCH = 0, 1, 2
 QEW_REQ_STATIC, QEW_REQ_LANGEVIN, QEW_REQ_DEPINNING = 0, 1, 2
 
 
@@ -170,6 +171,9 @@ _SIGS = {
     "qew_gradient_batch": (I, [VP, VP, I, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_measure_fp64_fma_rate": (I, [VP, I, PD, PD]),
     "qew_ctx_set_barrier_limits": (I, [VP, C.c_longlong, I]),
+    "qew_ctx_set_autotune": (I, [VP, I]),
+    "qew_ctx_force_tune_candidate": (I, [VP, I, I]),
+    "qew_tune_report": (I, [C.c_char_p, I]),
     "qew_gradient_host": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_gradient_host_batch": (I, [VP, VP, I, VP, I, C.POINTER(qew_params), I, VP]),
     "qew_split_heights": (I, [VP, VP, VP, I, VP, VP]),

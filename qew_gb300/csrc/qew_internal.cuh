@@ -43,6 +43,10 @@ struct qew_ctx {
     // that tests inject to make the waits run out)
     long long barrier_polls = 1LL << 26;
     int barrier_skip = -1;
+    // launch-shape autotuning (qew_tune.cuh): on by default; tune_force[k]
+    // >= 0 fixes kernel k's candidate (kernel ids of qew_tune.cuh)
+    int autotune = 1;
+    int tune_force[3] = {-1, -1, -1};
     std::string last_error;
     // copy streams and slot events of the host-buffer batch pipeline
     // (created on first use)

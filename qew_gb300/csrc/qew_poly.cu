@@ -24,18 +24,12 @@
 
 #include "qew_internal.cuh"
 #include "qew_poly.cuh"
+#include "qew_tune.cuh"
 
 namespace {
 
 constexpr int kBS = 256;
-#ifndef QEW_POLY_ITEMS
-#define QEW_POLY_ITEMS 2
-#endif
-#ifndef QEW_POLY_MIN_CTAS
-#define QEW_POLY_MIN_CTAS 4
-#endif
-constexpr int kItems = QEW_POLY_ITEMS;
-constexpr int kTile = kBS * kItems;
+constexpr int kMinCtas = 4;  // 64 registers a thread: up to 4 resident CTAs per SM
 
 struct PolyGeom {
     const double *poly;   // [ny][nx][4]
@@ -71,9 +65,10 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
-template <bool kArc>
-__global__ void __launch_bounds__(kBS, QEW_POLY_MIN_CTAS)
+template <bool kArc, int kItems>
+__global__ void __launch_bounds__(kBS, kMinCtas)
 k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ grad, int count) {
+    constexpr int kTile = kBS * kItems;
     __shared__ double s_h[2][kTile + 2];
     __shared__ double s_dv[kTile + 1];
     __shared__ double s_sl[kArc ? kTile + 1 : 1];
@@ -211,31 +206,38 @@ qew_status qew_gradient_poly_enqueue(qew_ctx *ctx, const qew_field *f, int count
     g.half_dx = 0.5 * g.L.dx;
     g.fdx = g.L.dx * p->driving_force;
     const bool arc = (p->model == QEW_MODEL_ARCLENGTH);
-    static const int per_sm[2] = {
-        [] {
-            int v = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_gradient_poly<false>, kBS, 0) !=
-                cudaSuccess) {
-                cudaGetLastError();
-                v = 1;
-            }
-            return std::max(1, v);
-        }(),
-        [] {
-            int v = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_gradient_poly<true>, kBS, 0) !=
-                cudaSuccess) {
-                cudaGetLastError();
-                v = 1;
-            }
-            return std::max(1, v);
-        }()};
-    const long long tiles = (long long)((n + kTile - 1) / kTile) * count;
-    if (tiles > INT_MAX) return qew_fail(ctx, QEW_ERR_INVALID, "gradient: more than 2^31 tiles");
-    const int grid = (int)std::min<long long>(tiles, (long long)per_sm[arc ? 1 : 0] * ctx->num_sms);
-    if (arc)
-        k_gradient_poly<true><<<grid, kBS, 0, ctx->stream>>>(d_h, g, d_grad, count);
-    else
-        k_gradient_poly<false><<<grid, kBS, 0, ctx->stream>>>(d_h, g, d_grad, count);
-    return qew_launch_check(ctx, "gradient_poly");
+    // Candidates: sites per thread {1, 2, 4} x resident CTAs per SM {2, 3, 4};
+    // every one computes the same numbers (the per-site arithmetic does not
+    // depend on the tiling). Hand-chosen default: 2 sites, 4 CTAs.
+    static const char *const names[9] = {"1 site x 2 CTA/SM", "1 site x 3 CTA/SM",
+                                          "1 site x 4 CTA/SM", "2 sites x 2 CTA/SM",
+                                          "2 sites x 3 CTA/SM", "2 sites x 4 CTA/SM",
+                                          "4 sites x 2 CTA/SM", "4 sites x 3 CTA/SM",
+                                          "4 sites x 4 CTA/SM"};
+    auto launch = [&](int c) -> qew_status {
+        const int items = 1 << (c / 3);
+        const int ctas = 2 + c % 3;
+        const long long tiles = (long long)((n + kBS * items - 1) / (kBS * items)) * count;
+        if (tiles > INT_MAX)
+            return qew_fail(ctx, QEW_ERR_INVALID, "gradient: more than 2^31 tiles");
+        const int grid = (int)std::min<long long>(tiles, (long long)ctas * ctx->num_sms);
+#define QEW_POLY_LAUNCH(A, I) \
+    k_gradient_poly<A, I><<<grid, kBS, 0, ctx->stream>>>(d_h, g, d_grad, count)
+        if (arc) {
+            if (items == 1) QEW_POLY_LAUNCH(true, 1);
+            else if (items == 2) QEW_POLY_LAUNCH(true, 2);
+            else QEW_POLY_LAUNCH(true, 4);
+        } else {
+            if (items == 1) QEW_POLY_LAUNCH(false, 1);
+            else if (items == 2) QEW_POLY_LAUNCH(false, 2);
+            else QEW_POLY_LAUNCH(false, 4);
+        }
+#undef QEW_POLY_LAUNCH
+        return qew_launch_check(ctx, "gradient_poly");
+    };
+    int cand = 5;
+    QEW_TRY(qew_tune_pick(ctx, kTuneGradientPoly,
+                          qew_tune_class((long long)n * count, arc ? 1 : 0), 9, 5, names, launch,
+                          &cand));
+    return launch(cand);
 }

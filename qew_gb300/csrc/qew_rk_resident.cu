@@ -16,6 +16,7 @@
 #include <algorithm>
 
 #include "qew_gridsync.cuh"
+#include "qew_tune.cuh"
 #include "qew_internal.cuh"
 #include "qew_noise32.cuh"
 #include "qew_rk_device.cuh"
@@ -138,8 +139,8 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
         const int sizes[3] = {8, 2, 1};
         const long long warps_per_sm[3] = {QEW_RK_WARPS_PER_SM / 2, QEW_RK_WARPS_PER_SM, 0};
         const long long half = n / 2;
-        const void *kern = nullptr;
-        int grid = 1;
+        int grids[3];
+        int heuristic = 2, grid_max = 1;
         for (int k = 0; k < 3; ++k) {
             int per_sm = 0;
             QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forms[k], kRkBS, 0));
@@ -147,15 +148,13 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
             if (ctx->warp_cap > 0) slots = std::min(slots, ctx->warp_cap / (kRkBS / 32));
             const long long budget = std::min<long long>(slots, warps_per_sm[k] * ctx->num_sms);
             const long long want = (half * sizes[k] + kRkBS - 1) / kRkBS;
-            if (want <= budget || k == 2) {
-                kern = forms[k];
-                grid = (int)std::max(1LL, std::min(want, (long long)slots));
-                break;
-            }
+            grids[k] = (int)std::max(1LL, std::min(want, (long long)std::max(slots, 1)));
+            grid_max = std::max(grid_max, grids[k]);
+            if (heuristic == 2 && k < 2 && want <= budget) heuristic = k;
         }
         // scratch: adv[n], partials[3*grid], sync word, result
         const size_t off_part = ((size_t)n * sizeof(double) + 255) & ~size_t(255);
-        const size_t off_sync = (off_part + 3 * (size_t)grid * sizeof(double) + 255) & ~size_t(255);
+        const size_t off_sync = (off_part + 3 * (size_t)grid_max * sizeof(double) + 255) & ~size_t(255);
         const size_t off_res = (off_sync + sizeof(GridSync) + 255) & ~size_t(255);
         QEW_TRY(qew_scratch_reserve(ctx, off_res + sizeof(qew_rk_result) + 256));
         char *base = (char *)ctx->scratch;
@@ -163,16 +162,59 @@ qew_status qew_rk_block_resident(qew_ctx *ctx, const qew_field *field, double *d
         double *part = (double *)(base + off_part);
         GridSync *sync = (GridSync *)(base + off_sync);
         qew_rk_result *d_res = (qew_rk_result *)(base + off_res);
-        QEW_CUDA(ctx, cudaMemsetAsync(adv, 0, (size_t)n * sizeof(double), ctx->stream));
-        QEW_TRY(qew_gridsync_init(ctx, sync));
         double lt = p->line_tension, fd = p->driving_force;
         int model = p->model;
-        void *args[] = {(void *)&nz, (void *)&d_h, (void *)&adv, (void *)&n, (void *)&dx,
-                        (void *)&lt, (void *)&fd, (void *)&model, (void *)&rk, (void *)&part,
-                        (void *)&sync, (void *)&d_res};
-        QEW_CUDA(ctx, cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kRkBS), args, 0,
-                                                  ctx->stream));
-        QEW_TRY(qew_launch_check(ctx, "rk_resident"));
+        auto run_form = [&](int k, double *hp, RkP rkk) -> qew_status {
+            QEW_CUDA(ctx, cudaMemsetAsync(adv, 0, (size_t)n * sizeof(double), ctx->stream));
+            QEW_TRY(qew_gridsync_init(ctx, sync));
+            void *args[] = {(void *)&nz, (void *)&hp, (void *)&adv, (void *)&n, (void *)&dx,
+                            (void *)&lt, (void *)&fd, (void *)&model, (void *)&rkk,
+                            (void *)&part, (void *)&sync, (void *)&d_res};
+            QEW_CUDA(ctx, cudaLaunchCooperativeKernel(forms[k], dim3(grids[k]), dim3(kRkBS), args,
+                                                      0, ctx->stream));
+            return qew_launch_check(ctx, "rk_resident");
+        };
+        // The search width: the autotuner times the three widths on the first
+        // call of a (line length, noise form, GPU share) class, each on a copy
+        // of this call's line for a few sweeps (every width gives the same
+        // lines bit for bit); the budget rule above is the default, replaced
+        // only by a width more than 20 % faster (a few sweeps sample a block
+        // whose work per sweep changes as it creeps).
+        static const char *const names[3] = {"8-lane groups", "lane pairs", "one lane"};
+        int noise_kind = 0;
+        if constexpr (std::is_same<N, NoiseSplit32>::value) noise_kind = 3;
+        else if constexpr (noise_is_ref<N>::value) noise_kind = 2;
+        else if constexpr (std::is_same<N, NoiseBSpline64>::value) noise_kind = nz.poly ? 1 : 0;
+        // The first sweeps of a block move many sites a long way (FP64-heavy)
+        // and the later ones few (latency-bound), and a block spends most of
+        // its sweeps in the later phase: the probe line is first advanced 24
+        // sweeps with the default width, then every candidate is timed for 8
+        // sweeps from that state.
+        double *tune_h = nullptr, *tune_start = nullptr;
+        RkP rk_probe = rk, rk_advance = rk;
+        rk_probe.max_sweeps = std::min(rk.max_sweeps, 8);
+        rk_advance.max_sweeps = std::min(rk.max_sweeps, 24);
+        auto probe = [&](int k) -> qew_status {
+            if (!tune_h) {
+                QEW_TRY(qew_alloc_async(ctx, (void **)&tune_h, (size_t)n * sizeof(double)));
+                QEW_TRY(qew_alloc_async(ctx, (void **)&tune_start, (size_t)n * sizeof(double)));
+                QEW_CUDA(ctx, cudaMemcpyAsync(tune_start, d_h, (size_t)n * sizeof(double),
+                                              cudaMemcpyDeviceToDevice, ctx->stream));
+                QEW_TRY(run_form(heuristic, tune_start, rk_advance));
+            }
+            QEW_CUDA(ctx, cudaMemcpyAsync(tune_h, tune_start, (size_t)n * sizeof(double),
+                                          cudaMemcpyDeviceToDevice, ctx->stream));
+            return run_form(k, tune_h, rk_probe);
+        };
+        int cand = heuristic;
+        const qew_status ts =
+            qew_tune_pick(ctx, kTuneRkSearch,
+                          qew_tune_class(n, 2 * noise_kind + (ctx->warp_cap > 0 ? 1 : 0)), 3,
+                          heuristic, names, probe, &cand, 0.2f);
+        if (tune_h) qew_free_async(tune_h, ctx->stream);
+        if (tune_start) qew_free_async(tune_start, ctx->stream);
+        QEW_TRY(ts);
+        QEW_TRY(run_form(cand, d_h, rk));
         GridSync hs;
         QEW_CUDA(ctx, cudaMemcpyAsync(res, d_res, sizeof(qew_rk_result), cudaMemcpyDeviceToHost,
                                       ctx->stream));

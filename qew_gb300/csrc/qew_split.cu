@@ -23,6 +23,7 @@
 #include "qew_internal.cuh"
 #include "qew_model_kernels.cuh"
 #include "qew_split.cuh"
+#include "qew_tune.cuh"
 
 namespace {
 
@@ -299,9 +300,11 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem) {
 // k_gradient_split, so the same results bit for bit. Used with the x-filtered
 // store, where it measured faster (60.7 vs 63.8 us for 8 lines of 2^20
 // points); with the 16-tap gather it measured slower (86.2 vs 81.4 us).
+template <int kItems>
 __global__ void __launch_bounds__(kBS, QEW_SPLIT_MIN_CTAS)
 k_gradient_split_persist(const int *__restrict__ hc, const float *__restrict__ hf, SplitGeom g,
                       float *__restrict__ grad, int count) {
+    constexpr int kTile = kBS * kItems;
     __shared__ int s_c[2][kTile + 2];
     __shared__ float s_f[2][kTile + 2];
     __shared__ float s_dv[kTile + 1];
@@ -423,21 +426,34 @@ SplitGeom qew_split_geom(const qew_field *f, int n, const qew_params *p) {
 // Split heights in, FP32 gradient out, `count` lines n apart.
 static qew_status split_launch(qew_ctx *ctx, const SplitGeom &g, int count, const int32_t *d_cell,
                                const float *d_frac, float *d_grad, const char *what) {
-    if (g.edge) {  // one persistent CTA per resident slot
-        static const int per_sm = [] {
-            int v = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_gradient_split_persist, kBS, 0) !=
-                cudaSuccess) {
-                cudaGetLastError();
-                v = 1;
-            }
-            return std::max(1, v);
-        }();
-        const long long tiles = (long long)((g.n + kTile - 1) / kTile) * count;
-        if (tiles > INT_MAX)
-            return qew_fail(ctx, QEW_ERR_INVALID, "%s: more than 2^31 tiles", what);
-        const int grid = (int)std::min<long long>(tiles, (long long)per_sm * ctx->num_sms);
-        k_gradient_split_persist<<<grid, kBS, 0, ctx->stream>>>(d_cell, d_frac, g, d_grad, count);
+    if (g.edge) {  // persistent CTAs, the launch shape chosen by the autotuner
+        // Candidates: sites per thread {1, 2} x resident CTAs per SM {4, 6, 8};
+        // the per-site arithmetic does not depend on them, so every candidate
+        // gives the same bits. Hand-chosen default: 2 sites x 8 CTAs.
+        static const char *const names[6] = {"1 site x 4 CTA/SM", "1 site x 6 CTA/SM",
+                                              "1 site x 8 CTA/SM", "2 sites x 4 CTA/SM",
+                                              "2 sites x 6 CTA/SM", "2 sites x 8 CTA/SM"};
+        auto launch = [&](int c) -> qew_status {
+            const int items = 1 + c / 3;
+            const int ctas = 4 + 2 * (c % 3);
+            const long long tiles =
+                (long long)((g.n + kBS * items - 1) / (kBS * items)) * count;
+            if (tiles > INT_MAX)
+                return qew_fail(ctx, QEW_ERR_INVALID, "%s: more than 2^31 tiles", what);
+            const int grid = (int)std::min<long long>(tiles, (long long)ctas * ctx->num_sms);
+            if (items == 1)
+                k_gradient_split_persist<1><<<grid, kBS, 0, ctx->stream>>>(d_cell, d_frac, g,
+                                                                           d_grad, count);
+            else
+                k_gradient_split_persist<2><<<grid, kBS, 0, ctx->stream>>>(d_cell, d_frac, g,
+                                                                           d_grad, count);
+            return qew_launch_check(ctx, what);
+        };
+        int cand = 5;
+        QEW_TRY(qew_tune_pick(ctx, kTuneGradientSplit,
+                              qew_tune_class((long long)g.n * count, g.arc), 6, 5, names, launch,
+                              &cand));
+        return launch(cand);
     } else {
         k_gradient_split<false, false>
             <<<dim3((g.n + kTile - 1) / kTile, count), kBS, 0, ctx->stream>>>(
