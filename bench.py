@@ -83,8 +83,8 @@ def parse():
     ap.add_argument("--dep-fstep", type=float, default=0.05)
     ap.add_argument("--dep-fmax", type=float, default=20.0)
     ap.add_argument("--dep-rate-sweeps", type=int, default=2000)
-    ap.add_argument("--serve-rates", default="100,300,1000,3000,10000")
-    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-rates", default="100,10000")
+    ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-inflight", type=int, default=32)
     ap.add_argument("--serve-lsteps", type=int, default=10000)
     return ap.parse_args()
@@ -704,61 +704,78 @@ def run_depinning(args, Q, torch):
 def run_serving(args, Q, torch):
     """Poisson request streams (seed 4) at each rate: 50% static minimise
     (FP64-refined to max|g| < 1e-8), 30% Langevin (serve_lsteps steps, T ~
-    U[0, 0.5], dt 0.01), 20% depinning f_c (ramp 0.05, bisection to 1e-3,
-    2000 sweeps per block); L log-uniform in [512, 65536] (even), 256 or 1024
+    U[0, 0.5], dt 0.01), 20% depinning f_c (line relaxed at f = 0, ramp 0.05,
+    bisection to 1e-2, 500 sweeps per block, FP32 velocities); L
+    log-uniform in [512, 65536] (even), 256 or 1024
     rows, xi ~ U[2, 8]; each field generated on the device per request;
-    admission by a 150 GB HBM budget; continuous batching over
-    serve_inflight workers."""
+    admission by a 150 GB HBM budget; static lines shorter than 2048 points
+    through the device-resident loop, the rest over serve_inflight workers.
+    Every rate serves the same request list (only the arrival times differ),
+    so the rates are compared on the same work."""
     rng = np.random.default_rng(4)
     rates = [float(x) for x in args.serve_rates.split(",") if x]
-    srv = Q.Server(hbm_budget_bytes=150e9, max_inflight=args.serve_inflight)
+    N = args.serve_requests
+    reqs = []
+    for k in range(N):
+        kind = int(rng.choice(3, p=[0.5, 0.3, 0.2]))
+        n = int(round(np.exp(rng.uniform(np.log(512), np.log(65536))) / 2)) * 2
+        r = dict(kind=kind, n=n, rows=int(rng.choice([256, 1024])),
+                 xi=float(rng.uniform(2, 8)), seed=100000 + k, model=int(rng.integers(0, 2)))
+        if kind == 1:
+            r.update(steps=args.serve_lsteps, temperature=float(rng.uniform(0, 0.5)), dt=0.01)
+        elif kind == 2:
+            r.update(model=0, f_step=0.05, f_max=5.0, bisect_rtol=1e-2, max_sweeps=500,
+                     max_advance=32.0, runaway=float(r["rows"]) / 4)
+        reqs.append(r)
+    gaps_unit = rng.exponential(1.0, N)
     out = {"metric": "serving latency p50/p99 and solves/s", "unit": "s",
-           "budget_GB": 150, "inflight": args.serve_inflight, "rates": [],
-           "mix": "50%% static (1e-8), 30%% Langevin (%d steps), 20%% depinning f_c"
-                  % args.serve_lsteps}
-    try:
-        for ri, rate in enumerate(rates):
-            N = args.serve_requests
-            reqs = []
-            for k in range(N):
-                kind = int(rng.choice(3, p=[0.5, 0.3, 0.2]))
-                n = int(round(np.exp(rng.uniform(np.log(512), np.log(65536))) / 2)) * 2
-                r = dict(kind=kind, n=n, rows=int(rng.choice([256, 1024])),
-                         xi=float(rng.uniform(2, 8)), seed=100000 * (ri + 1) + k,
-                         model=int(rng.integers(0, 2)))
-                if kind == 1:
-                    r.update(steps=args.serve_lsteps, temperature=float(rng.uniform(0, 0.5)),
-                             dt=0.01)
-                elif kind == 2:
-                    r.update(model=0, f_step=0.05, f_max=5.0, bisect_rtol=1e-3, max_sweeps=2000,
-                             max_advance=32.0, runaway=float(r["rows"]) / 4)
-                reqs.append(r)
-            gaps = rng.exponential(1.0 / rate, N)
+           "budget_GB": 150, "inflight": args.serve_inflight, "requests_per_rate": N,
+           "rates": [],
+           "mix": "50%% static (1e-8), 30%% Langevin (%d steps), 20%% depinning f_c "
+                  "(relaxed start, ramp 0.05, bisection to 1e-2, 500 sweeps per block)"
+                  % args.serve_lsteps,
+           "request_counts": {name: int(sum(r["kind"] == kind for r in reqs))
+                              for kind, name in ((0, "static"), (1, "langevin"),
+                                                 (2, "depinning"))},
+           "static_on_device_loop": int(sum(r["kind"] == 0 and r["n"] < 2048 for r in reqs))}
+    for rate in rates:
+        srv = Q.Server(hbm_budget_bytes=150e9, max_inflight=args.serve_inflight)
+        try:
+            gaps = gaps_unit / rate
             t_next = srv.clock()
             for k in range(N):
                 t_next += gaps[k]
                 while srv.clock() < t_next:
                     time.sleep(min(1e-3, max(0.0, t_next - srv.clock())))
                 srv.submit(**reqs[k])
+            t_last_submit = srv.clock()
             srv.drain(3600)
             resps = srv.poll(N + 16)
-            log("  serving rate %g: %d responses" % (rate, len(resps)))
-            lat = np.array([r["t_end"] - r["t_submit"] for r in resps])
-            span = max(r["t_end"] for r in resps) - min(r["t_submit"] for r in resps)
-            per_kind = {}
-            for kind, name in ((0, "static"), (1, "langevin"), (2, "depinning")):
-                lk = [r["t_end"] - r["t_submit"] for r in resps if r["kind"] == kind]
-                if lk:
-                    per_kind[name] = {"count": len(lk), "p50_s": float(np.percentile(lk, 50)),
-                                      "p99_s": float(np.percentile(lk, 99))}
-            out["rates"].append({
-                "rate_per_s": rate, "requests": N, "ok": int(sum(r["status"] == 0 for r in resps)),
-                "static_converged_1e8": int(sum(r["kind"] == 0 and r["converged"] and
-                                                r["max_force"] < 1e-8 for r in resps)),
-                "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-                "solves_per_s": N / span, "per_kind": per_kind})
-    finally:
-        srv.close()
+            lane = srv.lane_stats()
+        finally:
+            srv.close()
+        log("  serving rate %g: %d responses" % (rate, len(resps)))
+        lat = np.array([r["t_end"] - r["t_submit"] for r in resps])
+        t0 = min(r["t_submit"] for r in resps)
+        span = max(r["t_end"] for r in resps) - t0
+        per_kind = {}
+        for kind, name in ((0, "static"), (1, "langevin"), (2, "depinning")):
+            lk = [r["t_end"] - r["t_submit"] for r in resps if r["kind"] == kind]
+            svc = [r["t_end"] - r["t_start"] for r in resps if r["kind"] == kind]
+            if lk:
+                per_kind[name] = {"count": len(lk), "p50_s": float(np.percentile(lk, 50)),
+                                  "p99_s": float(np.percentile(lk, 99)),
+                                  "service_p50_s": float(np.percentile(svc, 50))}
+        out["rates"].append({
+            "rate_per_s": rate, "requests": N, "arrival_span_s": t_last_submit - t0,
+            "ok": int(sum(r["status"] == 0 for r in resps)),
+            "static_converged_1e8": int(sum(r["kind"] == 0 and r["converged"] and
+                                            r["max_force"] < 1e-8 for r in resps)),
+            "depinning_with_f_c": int(sum(r["kind"] == 2 and r["converged"] for r in resps)),
+            "service_s_total": float(sum(r["t_end"] - r["t_start"] for r in resps)),
+            "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "solves_per_s": N / span, "makespan_s": span, "per_kind": per_kind,
+            "device_loop": lane})
     return out
 
 

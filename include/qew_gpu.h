@@ -474,6 +474,18 @@ int qew_server_poll(qew_server *s, qew_response *out, int max);
 /* Waits until the queue is empty and nothing runs (QEW_ERR_TIMEOUT). */
 qew_status qew_server_drain(qew_server *s, double timeout_s);
 double qew_server_clock(const qew_server *s);
+/* The device-resident loop for static requests (no reference counterpart):
+ * static requests on lines shorter than 2048 points at ftol 1e-8 are not
+ * given to a worker; a persistent grid (one CTA per SM) takes them from a
+ * ring in mapped host memory as the host publishes them and relaxes each on
+ * one CTA (FP32 phase, FP64 refinement, the ensemble's arithmetic), so they
+ * join running work without a launch of their own. A CTA without work for
+ * about 16 ms leaves; the server relaunches the grid when jobs wait. Longer
+ * lines take a thread-block cluster through a worker. *served: requests the
+ * loop has finished; *launches: launches of its grid. QEW_ERR_UNSUPPORTED
+ * when the loop could not be set up (all requests then go to workers). */
+qew_status qew_server_lane_stats(qew_server *s, uint64_t *served,
+                                 uint64_t *launches);
 qew_status qew_server_destroy(qew_server *s);
 
 /* --------------------------------------------------------------- Langevin */

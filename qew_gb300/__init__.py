@@ -994,6 +994,13 @@ class Server:
                      t_start=b.t_start, t_end=b.t_end, iterations=b.iterations, value=b.value,
                      max_force=b.max_force, converged=bool(b.converged)) for b in buf[:k]]
 
+    def lane_stats(self) -> dict:
+        """Requests served by the device-resident static loop, and its launches."""
+        served, launches = C.c_uint64(), C.c_uint64()
+        st = self.lib.qew_server_lane_stats(self.h, C.byref(served), C.byref(launches))
+        return {"available": st == _capi.QEW_OK, "served": served.value,
+                "launches": launches.value}
+
     def drain(self, timeout_s: float = 600.0) -> None:
         _capi.check(self.lib.qew_server_drain(self.h, float(timeout_s)), None, "drain")
 

@@ -186,3 +186,224 @@ extern "C" qew_status qew_ensemble_minimize(qew_ctx *ctx, int count, const qew_e
     QEW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return QEW_OK;
 }
+
+// ------------------------------------------------------------ serving lane
+// A device-resident request loop for static lines (qew_serve_lane.cuh): a
+// persistent grid whose CTAs claim jobs from a ring in mapped host memory as
+// the host publishes them, relax each like one ensemble line (FP32 phase,
+// FP64 refinement), and post the result back to the ring. Every wait is
+// bounded: a CTA that finds no work for idle_polls polls leaves, and the
+// host relaunches the grid when jobs remain unclaimed.
+#include "qew_serve_lane.cuh"
+
+namespace {
+
+struct LaneRing {  // mapped pinned host memory
+    EnsJob jobs[kLaneRing];
+    qew_lbfgs_result results[kLaneRing];
+    unsigned long long done[kLaneRing];  // k + 1 once job k's result is posted
+    unsigned int published;              // jobs [0, published) are readable
+    int closing;                         // set by the host to let the grid leave
+};
+static_assert(sizeof(EnsJob) % 8 == 0, "EnsJob is copied in 8-byte words");
+
+__device__ __forceinline__ unsigned int ld_acquire_sys_u32(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(kEnsBS, 2)
+k_serve_static(LaneRing *ring, unsigned int *head, LbfgsCfg cfg32, LbfgsCfg cfg64, int use32,
+               double *ws_base, size_t ws_per_cta, long long idle_polls) {
+    __shared__ int s_k;
+    __shared__ EnsJob s_job;
+    double *ws = ws_base + (size_t)blockIdx.x * ws_per_cta;
+    for (;;) {  // each pass claims one job or leaves; a solve is bounded by max_iter
+        if (threadIdx.x == 0) {
+            int k = -1;
+            long long polls = 0;
+            while (polls <= idle_polls) {
+                const unsigned int pub = ld_acquire_sys_u32(&ring->published);
+                const unsigned int h = *(volatile unsigned int *)head;
+                if (h < pub) {
+                    if (atomicCAS(head, h, h + 1u) == h) {
+                        k = (int)h;
+                        break;
+                    }
+                    ++polls;  // another CTA took it: counts toward the bound
+                    continue;
+                }
+                if (*(volatile int *)&ring->closing) break;
+                ++polls;
+                __nanosleep(1000);
+            }
+            if (k >= 0) {
+                const volatile unsigned long long *src =
+                    (const volatile unsigned long long *)&ring->jobs[k % kLaneRing];
+                unsigned long long *dst = (unsigned long long *)&s_job;
+                for (int w = 0; w < (int)(sizeof(EnsJob) / 8); ++w) dst[w] = src[w];
+            }
+            s_k = k;
+        }
+        __syncthreads();
+        const int k = s_k;
+        if (k < 0) break;
+        const EnsJob j = s_job;
+        __syncthreads();
+        const size_t npad = ((size_t)j.n + 31) & ~size_t(31);
+        qew_lbfgs_result r32{};
+        if (use32)
+            r32 = lbfgs_block<NoiseSplit32, kEnsBS, float>(job_noise32(j), j.h, j.n, j.p, cfg32,
+                                                           j.pc, ws, npad);
+        qew_lbfgs_result r =
+            lbfgs_block<NoiseBSpline64, kEnsBS>(job_noise64(j), j.h, j.n, j.p, cfg64, j.pc, ws, npad);
+        if (threadIdx.x == 0) {
+            r.iterations += r32.iterations;
+            r.n_func_evals += r32.n_func_evals;
+            r.n_curvature_skips += r32.n_curvature_skips;
+            r.n_ls_restarts += r32.n_ls_restarts;
+            ring->results[k % kLaneRing] = r;
+            __threadfence_system();
+            *(volatile unsigned long long *)&ring->done[k % kLaneRing] =
+                (unsigned long long)k + 1ull;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+struct StaticLane {
+    int device = 0;
+    cudaStream_t stream = nullptr;  // the lane kernel's stream
+    LaneRing *ring = nullptr;       // host address
+    LaneRing *ring_d = nullptr;     // device address of the same memory
+    unsigned int *head = nullptr;   // device: jobs claimed so far
+    double *ws = nullptr;
+    size_t ws_per_cta = 0;
+    int grid = 0, nmax = 0, use32 = 0;
+    LbfgsCfg cfg32{}, cfg64{};
+    long long idle_polls = 1 << 14;  // about 16 ms of polls without work
+    cudaEvent_t done_ev = nullptr;
+    bool running = false;
+    unsigned int published = 0;
+    uint64_t launches = 0;
+};
+
+qew_status qew_lane_create(int device, int nmax, const qew_lbfgs_params *lp, double ftol32,
+                           int ctas, StaticLane **out) {
+    if (!out || !lp || nmax < 1 || ctas < 1 || lp->m < 1 || lp->m > kLbfgsMaxM)
+        return QEW_ERR_INVALID;
+    StaticLane *L = new (std::nothrow) StaticLane();
+    if (!L) return QEW_ERR_NOMEM;
+    L->device = device;
+    L->nmax = nmax;
+    L->grid = ctas;
+    L->use32 = ftol32 > 0 ? 1 : 0;
+    L->cfg64 = lbfgs_cfg_from(lp);
+    L->cfg32 = L->cfg64;
+    L->cfg32.ftol = ftol32;
+    const size_t npad_max = ((size_t)nmax + 31) & ~size_t(31);
+    L->ws_per_cta = npad_max * (size_t)(kLbfgsVecs + 2 * (lp->m + 1));
+    auto fail = [&](qew_status s) {
+        if (L->ws) cudaFree(L->ws);
+        if (L->head) cudaFree(L->head);
+        if (L->ring) cudaFreeHost(L->ring);
+        if (L->stream) cudaStreamDestroy(L->stream);
+        if (L->done_ev) cudaEventDestroy(L->done_ev);
+        cudaGetLastError();
+        delete L;
+        return s;
+    };
+    if (cudaSetDevice(device) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&L->done_ev, cudaEventDisableTiming) != cudaSuccess)
+        return fail(QEW_ERR_CUDA);
+    if (cudaHostAlloc((void **)&L->ring, sizeof(LaneRing), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer((void **)&L->ring_d, L->ring, 0) != cudaSuccess ||
+        cudaMalloc((void **)&L->head, sizeof(unsigned int)) != cudaSuccess ||
+        cudaMalloc((void **)&L->ws, L->ws_per_cta * (size_t)ctas * sizeof(double)) != cudaSuccess)
+        return fail(QEW_ERR_NOMEM);
+    memset((void *)L->ring, 0, sizeof(LaneRing));
+    if (cudaMemset(L->head, 0, sizeof(unsigned int)) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess)
+        return fail(QEW_ERR_CUDA);
+    *out = L;
+    return QEW_OK;
+}
+
+qew_status qew_lane_publish(StaticLane *L, const qew_field *f, double *d_h, int n,
+                            const qew_params *p, double shift, unsigned int *k) {
+    if (!L || !f || !d_h || !p || n < 1 || n > L->nmax || f->kind != QEW_FIELD_BSPLINE ||
+        !f->coef64 || (L->use32 && !f->coef32))
+        return QEW_ERR_INVALID;
+    EnsJob j{};
+    j.coef64 = f->coef64;
+    j.poly64 = f->poly64;
+    j.ky = make_bspline64(f).ky;
+    j.coef32 = f->coef32;
+    j.edge32 = f->edge32;
+    j.nx = f->nx;
+    j.ny = f->ny;
+    j.fdx = f->dx;
+    j.fdy = f->dy;
+    j.Lx = f->Lx;
+    j.h = d_h;
+    j.n = n;
+    j.p = *p;
+    j.pc = L->cfg64.precondition ? qew_precond_coef(n, p->line_tension, p->physical_size, shift)
+                                 : PrecondCoef{};
+    const unsigned int idx = L->published;
+    L->ring->jobs[idx % kLaneRing] = j;
+    __atomic_store_n(&L->ring->published, idx + 1u, __ATOMIC_RELEASE);
+    L->published = idx + 1u;
+    *k = idx;
+    return QEW_OK;
+}
+
+qew_status qew_lane_pump(StaticLane *L, cudaStream_t aux) {
+    if (!L) return QEW_ERR_INVALID;
+    if (L->running) {
+        const cudaError_t q = cudaEventQuery(L->done_ev);
+        if (q == cudaErrorNotReady) return QEW_OK;
+        if (q != cudaSuccess) return QEW_ERR_CUDA;
+        L->running = false;
+    }
+    unsigned int claimed = 0;
+    if (cudaMemcpyAsync(&claimed, L->head, sizeof(unsigned int), cudaMemcpyDeviceToHost, aux) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(aux) != cudaSuccess)
+        return QEW_ERR_CUDA;
+    if (claimed >= L->published) return QEW_OK;  // nothing waits
+    k_serve_static<<<L->grid, kEnsBS, 0, L->stream>>>(L->ring_d, L->head, L->cfg32, L->cfg64,
+                                                      L->use32, L->ws, L->ws_per_cta,
+                                                      L->idle_polls);
+    if (cudaGetLastError() != cudaSuccess) return QEW_ERR_CUDA;
+    if (cudaEventRecord(L->done_ev, L->stream) != cudaSuccess) return QEW_ERR_CUDA;
+    L->running = true;
+    ++L->launches;
+    return QEW_OK;
+}
+
+bool qew_lane_done(StaticLane *L, unsigned int k, qew_lbfgs_result *r) {
+    const unsigned long long d = __atomic_load_n(&L->ring->done[k % kLaneRing], __ATOMIC_ACQUIRE);
+    if (d != (unsigned long long)k + 1ull) return false;
+    *r = L->ring->results[k % kLaneRing];
+    return true;
+}
+
+uint64_t qew_lane_launches(const StaticLane *L) { return L ? L->launches : 0; }
+
+void qew_lane_destroy(StaticLane *L) {
+    if (!L) return;
+    cudaSetDevice(L->device);
+    __atomic_store_n(&L->ring->closing, 1, __ATOMIC_RELEASE);
+    cudaStreamSynchronize(L->stream);  // every CTA leaves at its next idle check
+    cudaFree(L->ws);
+    cudaFree(L->head);
+    cudaFreeHost(L->ring);
+    cudaEventDestroy(L->done_ev);
+    cudaStreamDestroy(L->stream);
+    delete L;
+}

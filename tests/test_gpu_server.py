@@ -82,3 +82,32 @@ def test_budget_admission_and_limits(Q):
                        bisect_rtol=1e-3, max_sweeps=100)
     finally:
         srv.close()
+
+
+def test_static_lane_equals_ensemble(Q):
+    """Short static requests go to the device-resident loop; each result is
+    the one-line ensemble solve's (same field, same settings) bit for bit."""
+    import torch
+    specs = [(512, 3.0, 21, 0), (1000, 2.5, 22, 1), (1536, 5.0, 23, 0), (2046, 4.0, 24, 1)]
+    reqs = [dict(kind=0, n=n, rows=256, xi=xi, seed=sd, model=m, ftol=1e-8)
+            for n, xi, sd, m in specs]
+    srv = Q.Server(hbm_budget_bytes=20e9, max_inflight=2)
+    lines = [np.zeros(r["n"]) for r in reqs]
+    try:
+        ids = [srv.submit(h_out=lines[k], **r) for k, r in enumerate(reqs)]
+        srv.drain(600)
+        got = {r["id"]: r for r in srv.poll()}
+        stats = srv.lane_stats()
+    finally:
+        srv.close()
+    assert stats["available"] and stats["served"] == len(reqs) and stats["launches"] >= 1
+    lp = Q.LbfgsParams(m=10, ftol=1e-8, max_iter=20000, precondition=True, ls_fallback=True)
+    for (n, xi, sd, m), k, h in zip(specs, ids, lines):
+        f = Q.FilteredNoise.generated(n, 256, float(n), 256.0, 1.0, xi, xi, sd,
+                                      store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+        p = Q.Params(float(n), 1.0, 0.0, Q.Model(m))
+        he = torch.zeros(n, dtype=torch.float64, device="cuda")
+        re = Q.ensemble_minimize([(he, p, f, 0.5 / xi ** 2)], lp, ftol_fp32=2e-5)[0]
+        assert got[k]["status"] == 0 and got[k]["iterations"] == re.iterations
+        assert np.array_equal(h, he.cpu().numpy())
+        assert got[k]["converged"] and got[k]["max_force"] < 1e-8
