@@ -60,6 +60,8 @@ def parse():
                     help="field without the x-filtered FP32 copy: the split gather reads the 16 "
                          "B-spline taps per edge (the form used on lines that do not have one "
                          "point per field column)")
+    ap.add_argument("--no-headline", action="store_true",
+                    help="run only the --sections configurations (profiling), no headline")
     ap.add_argument("--profile-run", action="store_true",
                     help="GPU timed loop only (no e2e, CPU baseline or clock sampling)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -814,6 +816,22 @@ def fp64_peak(Q, ctx):
 FP64_INST_PER_POINT = {"k_gradient_poly": 8.0, "k_gradient": 49.15}
 
 
+def run_sections_only(args, Q, torch, rank):
+    """The --sections configurations without the headline measurement: one
+    JSON line of their results (for profiling a section's kernels)."""
+    runners = {"refshape": run_reference_shape, "static": run_static,
+               "ensemble": run_ensemble, "dynamics": run_dynamics,
+               "depinning": run_depinning, "serving": run_serving}
+    out = {}
+    for name in [x.strip() for x in args.sections.split(",") if x.strip()]:
+        log("%s section" % name)
+        out[name] = runners[name](args, Q, torch)
+        torch.cuda.empty_cache()
+    if rank == 0:
+        print(json.dumps({"sections": out}), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     ws, rank, local = dist_env()
@@ -825,6 +843,8 @@ def run_ours(args):
     qbuild.build()
     import qew_gb300 as Q
 
+    if args.no_headline:  # one configuration section alone (profiling runs)
+        return run_sections_only(args, Q, torch, rank)
     if args.small:
         L, ny, n_inst = L_FULL, 64, N_INST
     else:
@@ -934,7 +954,7 @@ def run_ours(args):
     # small field (each point touches the same number of rows whatever the
     # field height), scaled to the points of one launch.
     dram_per_point = {
-        "k_gradient_poly": (342.752256e6 + 52.867072e6) / (8 * L_FULL),
+        "k_gradient_poly": (342.742272e6 + 51.131904e6) / (8 * L_FULL),
         "k_gradient_split_persist": (237.686784e6 + 22.566656e6) / (8 * L_FULL),
         "k_gradient_split": (241.858816e6 + 20.879104e6) / (8 * L_FULL),
         "k_gradient": (43.320832e6 + 0.039936e6) / L_FULL,
