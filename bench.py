@@ -85,6 +85,8 @@ def parse():
     ap.add_argument("--dep-fstep", type=float, default=0.05)
     ap.add_argument("--dep-fmax", type=float, default=20.0)
     ap.add_argument("--dep-rate-sweeps", type=int, default=2000)
+    ap.add_argument("--dep-forms", default="fp64,fp64_poly,fp32split",
+                    help="velocity forms of the depinning section")
     ap.add_argument("--serve-rates", default="100,10000")
     ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-inflight", type=int, default=32)
@@ -619,10 +621,12 @@ def run_depinning(args, Q, torch):
     cell-polynomial store, and from the FP32 coefficients; the plain
     host-driven form is timed on one block for its sweep rate."""
     n = ny = args.dep_size
+    dep_forms = [x.strip() for x in args.dep_forms.split(",") if x.strip()]
     fld = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2,
                                     store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
-    fld_poly = Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2,
-                                         store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY)
+    fld_poly = (Q.FilteredNoise.generated(n, ny, float(n), float(ny), 1.0, 4.0, 4.0, 2,
+                                          store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY)
+                if "fp64_poly" in dep_forms else None)
     rp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
                     runaway=2.0 * ny, max_sweeps=args.dep_max_sweeps)
     out = {"metric": "time to f_c (ramp + bisection to 1e-10)", "unit": "s",
@@ -630,6 +634,8 @@ def run_depinning(args, Q, torch):
     crit = {}
     for name, prec in (("fp64", Q.QEW_PREC_FP64), ("fp64_poly", Q.QEW_PREC_FP64),
                        ("fp32split", Q.QEW_PREC_FP32_SPLIT)):
+        if name not in dep_forms:
+            continue
         fld_k = fld_poly if name == "fp64_poly" else fld
         h = torch.full((n,), 0.5 * ny, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
@@ -674,6 +680,8 @@ def run_depinning(args, Q, torch):
         out["fp32_vs_fp64"] = {
             "f_c_rel_diff": abs(out["fp32split"]["f_c"] - out["fp64"]["f_c"]) / out["fp64"]["f_c"],
             "max_abs_h_diff_critical": float((crit["fp64"] - crit["fp32split"]).abs().max())}
+
+    if "fp64" in crit:
         # sweep rate: resident vs plain host-driven, one block at the last blocked force
         p_lo = Q.Params(float(n), 1.0, out["fp64"]["f_lo"], Q.Model.Linear)
         rates = {}
@@ -682,6 +690,8 @@ def run_depinning(args, Q, torch):
                 ("resident_poly", Q.QEW_RK_RESIDENT, fld_poly, Q.QEW_PREC_FP64),
                 ("resident_reference_exact", Q.QEW_RK_RESIDENT, fld, Q.QEW_PREC_FP64_REFERENCE),
                 ("plain", Q.QEW_RK_PLAIN, fld, Q.QEW_PREC_FP64)):
+            if fk is None:
+                continue
             rpp = Q.RkParams(dstep=0.5, max_advance=float(ny), root_tol=1e-10, sweep_tol=1e-8,
                              runaway=2.0 * ny, max_sweeps=args.dep_rate_sweeps)
             # one untimed block first: a class's first call runs the autotuner's probe
