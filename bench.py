@@ -865,7 +865,13 @@ def run_ours(args):
         store |= Q.QEW_STORE_FP32_EDGE
     if not args.no_poly_store:
         store |= Q.QEW_STORE_FP64_POLY
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter()
     noise = Q.FilteredNoise(field, float(L), float(ny), store=store)
+    torch.cuda.synchronize()
+    field_setup = {"ms": 1e3 * (time.perf_counter() - t_setup),
+                   "what": "prefilter of the resident field and every store the run reads "
+                           "(FP64, FP32, x-filtered FP32, FP64 cell polynomials as selected)"}
     del field
     torch.cuda.empty_cache()
     rng = np.random.default_rng(SEED + 1000 * rank)
@@ -911,6 +917,16 @@ def run_ours(args):
                       "k_gradient_split" if args.no_edge_store else "k_gradient_split_persist",
                       "f32"),
     }
+    # The energy of the same lines, objective() once per line (each call
+    # reads its scalar back to the host, as the reference's reduction does):
+    # 40 B per point algorithmic (the 4 field rows' 32 B and the height).
+    energies = np.empty(n_inst)
+
+    def step_objective():
+        for k in range(n_inst):
+            energies[k] = Q.objective(H[k], p, noise)
+
+    forms_extra = {"objective_fp64": (step_objective, 40.0, "k_objective", "f64")}
     head = args.precision
     warm = max(args.warmup, 3)
     for _ in range(warm):
@@ -970,7 +986,7 @@ def run_ours(args):
         "k_gradient": (43.320832e6 + 0.039936e6) / L_FULL,
     }
     results = {}
-    for name, (fn, bpp, kern, dt) in forms.items():
+    for name, (fn, bpp, kern, dt) in list(forms.items()) + list(forms_extra.items()):
         if name == head:
             ms, nl, val = t_ms, launches, value
         else:
@@ -1070,7 +1086,7 @@ def run_ours(args):
                 "config": headline_config(L, ny, n_inst, head, ws),
                 "roofline": head_r["roofline"], "fp64_roofline": head_r["fp64_roofline"],
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
-                "forms": {k: v for k, v in results.items() if k != head},
+                "field_setup": field_setup, "forms": {k: v for k, v in results.items() if k != head},
                 "autotune": [ln for ln in Q.tune_report().splitlines() if ln],
                 "reference_shape": refshape, "static": static, "ensemble": ensemble,
                 "dynamics": dynamics,

@@ -614,6 +614,18 @@ qew_status qew_ctx_force_tune_candidate(qew_ctx *ctx, int kernel, int candidate)
  * returns the full length. */
 int qew_tune_report(char *buf, int size);
 
+/* ------------------------------------------------------- bounds checking */
+/* The library built with -DQEW_BOUNDS_CHECK (qew_gb300/build.py, variant
+ * "bounds_check", in _lib/bounds_check/) range-checks every field gather and
+ * the gradient kernels' shared-memory indices on the device; an index
+ * outside its array is clamped into range and recorded. No reference
+ * counterpart (it stands in for a memory checker). Fills out[0] = the number
+ * of out-of-range indices since the last report, out[1] = the first such
+ * index, out[2] = its bound, out[3] = the source line of the check, after
+ * synchronising the device, and clears them. QEW_ERR_UNSUPPORTED in the
+ * normal build. */
+qew_status qew_bounds_check_report(long long out[4]);
+
 /* ------------------------------------------------------------ measurement */
 /* FP64 FMA instructions per second of this GPU (no reference counterpart: the
  * roof of the FP64-pipe-bound gather). Eight resident CTAs per SM, each

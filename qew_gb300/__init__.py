@@ -200,6 +200,17 @@ def tune_report() -> str:
     return buf.value.decode()
 
 
+def bounds_check_report() -> dict | None:
+    """Out-of-range device indices since the last call (qew_bounds_check_report):
+    {"count", "index", "bound", "line"}; None in the normal (unchecked) build."""
+    out = (C.c_longlong * 4)()
+    st = _capi.load().qew_bounds_check_report(out)
+    if st == _capi.QEW_ERR_UNSUPPORTED:
+        return None
+    _capi.check(st, None, "bounds_check_report")
+    return dict(zip(("count", "index", "bound", "line"), (int(v) for v in out)))
+
+
 _contexts: dict[int, Context] = {}
 
 

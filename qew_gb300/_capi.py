@@ -10,7 +10,9 @@ import os
 import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libqew_gb300.so")
+# QEW_GB300_VARIANT=bounds_check loads the bounds-checked build (_lib/bounds_check/)
+_VARIANT = os.environ.get("QEW_GB300_VARIANT", "")
+LIB_PATH = os.path.join(HERE, "_lib", *((_VARIANT,) if _VARIANT else ()), "libqew_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "qew_gpu.h")
 HEADERS = [HEADER, os.path.join(os.path.dirname(HERE), "include", "qew_runs.h")]
 
@@ -172,6 +174,7 @@ _SIGS = {
     "qew_measure_fp64_fma_rate": (I, [VP, I, PD, PD]),
     "qew_ctx_set_barrier_limits": (I, [VP, C.c_longlong, I]),
     "qew_ctx_set_autotune": (I, [VP, I]),
+    "qew_bounds_check_report": (I, [C.POINTER(C.c_longlong)]),
     "qew_ctx_force_tune_candidate": (I, [VP, I, I]),
     "qew_tune_report": (I, [C.c_char_p, I]),
     "qew_gradient_host": (I, [VP, VP, VP, I, C.POINTER(qew_params), I, VP]),

@@ -83,18 +83,33 @@ def _stale(lib: str, srcs) -> bool:
     return any(os.path.getmtime(s) > t for s in list(srcs) + _headers() + [__file__])
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
+def build(force: bool = False, verbose: bool = False, extra_flags=None,
+          variant: str = "") -> str:
+    """Build the library (variant "bounds_check": the range-checked build in
+    _lib/bounds_check/, without the executables)."""
+    if variant:
+        if variant != "bounds_check":
+            raise ValueError("unknown build variant %r" % variant)
+        return _build_lib(force, verbose, list(extra_flags or []) + ["-DQEW_BOUNDS_CHECK"],
+                          os.path.join(OUT_DIR, variant), executables=False)
+    return _build_lib(force, verbose, extra_flags, OUT_DIR, executables=True)
+
+
+def _build_lib(force, verbose, extra_flags, out_dir, executables) -> str:
+    lib_path = os.path.join(out_dir, "libqew_gb300.so")
+    obj_dir = os.path.join(out_dir, "obj")
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    if not force and not _stale(LIB, srcs):
-        _build_executables(force)
-        return LIB
+    if not force and not _stale(lib_path, srcs):
+        if executables:
+            _build_executables(force)
+        return lib_path
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
-    os.makedirs(OBJ_DIR, exist_ok=True)
+    os.makedirs(obj_dir, exist_ok=True)
     flags = ARCH + NVCC_FLAGS + ["-I" + INCLUDE] + list(extra_flags or [])
 
     def compile_one(src):
-        obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
+        obj = os.path.join(obj_dir, os.path.basename(src) + ".o")
         cmd = [nvcc] + flags + ["-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -107,16 +122,18 @@ def build(force: bool = False, verbose: bool = False, extra_flags=None) -> str:
     with cf.ThreadPoolExecutor(workers) as ex:
         objs = list(ex.map(compile_one, srcs))
     libdir = os.path.join(cuda, "lib64")
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib_path + ".tmp%d" % os.getpid()
     cmd = [nvcc] + ARCH + ["-shared", "-o", tmp] + objs + [
         "-L" + libdir, "-lcufft", "-Xlinker", "-rpath," + libdir]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
-    os.replace(tmp, LIB)
-    _build_executables(True)
-    return LIB
+    os.replace(tmp, lib_path)
+    if executables:
+        _build_executables(True)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+                variant="bounds_check" if "--bounds-check" in sys.argv else ""))

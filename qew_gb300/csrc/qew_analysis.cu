@@ -52,6 +52,7 @@ __global__ void k_acf(const double *__restrict__ r, long lines, int n, int nh, d
 extern "C" qew_status qew_line_statistics(qew_ctx *ctx, int count, const double *d_h, int n,
                                           double physical_size, double *d_ell, double *d_acf,
                                           double *d_q, double *d_psd) {
+    QEW_RANGE();
     if (!ctx || count < 1 || !d_h || n < 2 || !(physical_size > 0) || (!d_acf && !d_psd))
         return qew_fail(ctx, QEW_ERR_INVALID, "line_statistics: bad arguments");
     QEW_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -103,6 +104,7 @@ extern "C" qew_status qew_line_statistics(qew_ctx *ctx, int count, const double 
 extern "C" qew_status qew_line_statistics_host(qew_ctx *ctx, int count, const double *h_h, int n,
                                                double physical_size, double *h_ell,
                                                double *h_acf, double *h_q, double *h_psd) {
+    QEW_RANGE();
     if (!ctx || count < 1 || !h_h || n < 2 || (!h_acf && !h_psd))
         return qew_fail(ctx, QEW_ERR_INVALID, "line_statistics_host: bad arguments");
     QEW_CUDA(ctx, cudaSetDevice(ctx->device));

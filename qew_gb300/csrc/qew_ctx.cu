@@ -159,3 +159,44 @@ const char *qew_last_error(const qew_ctx *ctx) {
 uint64_t qew_ctx_launch_count(const qew_ctx *ctx) { return ctx ? ctx->launches : 0; }
 
 }  // extern "C"
+
+#ifdef QEW_BOUNDS_CHECK
+#include <mutex>
+namespace {
+std::mutex g_bounds_mu;
+unsigned long long *g_bounds_host = nullptr, *g_bounds_dev = nullptr;
+}  // namespace
+
+unsigned long long *qew_bounds_words() {
+    std::lock_guard<std::mutex> lock(g_bounds_mu);
+    if (!g_bounds_host) {
+        if (cudaHostAlloc((void **)&g_bounds_host, 4 * sizeof(unsigned long long),
+                          cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&g_bounds_dev, g_bounds_host, 0) != cudaSuccess) {
+            cudaGetLastError();
+            g_bounds_host = nullptr;
+            return nullptr;
+        }
+        memset(g_bounds_host, 0, 4 * sizeof(unsigned long long));
+    }
+    return g_bounds_dev;
+}
+#endif
+
+extern "C" qew_status qew_bounds_check_report(long long out[4]) {
+#ifdef QEW_BOUNDS_CHECK
+    if (!out) return QEW_ERR_INVALID;
+    qew_bounds_words();
+    std::lock_guard<std::mutex> lock(g_bounds_mu);
+    if (!g_bounds_host) return QEW_ERR_CUDA;
+    cudaDeviceSynchronize();
+    for (int k = 0; k < 4; ++k) {
+        out[k] = (long long)__atomic_load_n(&g_bounds_host[k], __ATOMIC_ACQUIRE);
+        g_bounds_host[k] = 0;
+    }
+    return QEW_OK;
+#else
+    (void)out;
+    return QEW_ERR_UNSUPPORTED;
+#endif
+}

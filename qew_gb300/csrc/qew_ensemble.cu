@@ -29,6 +29,9 @@ struct EnsJob {
     const double *coef64;
     const double *poly64;  // FP64 cell-polynomial store, or null
     int ky;                // y * 2^ky == y / dy, or kPolyNotPow2
+#ifdef QEW_BOUNDS_CHECK
+    unsigned long long *oob;
+#endif
     const float *coef32;
     const float *edge32;
     int nx, ny;
@@ -57,6 +60,9 @@ __device__ __forceinline__ NoiseBSpline64 job_noise64(const EnsJob &j) {
     nz.wxc[3] = 0.125 * (1.0 / 6.0);
     nz.poly = (j.n == j.nx && j.p.physical_size == j.Lx) ? j.poly64 : nullptr;
     nz.ky = j.ky;
+#ifdef QEW_BOUNDS_CHECK
+    nz.oob = j.oob;
+#endif
     return nz;
 }
 
@@ -74,6 +80,9 @@ __device__ __forceinline__ NoiseSplit32 job_noise32(const EnsJob &j) {
     nz.xconst = (j.n == j.nx && j.p.physical_size == j.Lx && nz.dx_pow2);
     nz.edge = nz.xconst ? j.edge32 : nullptr;
     nz.inv_dy_f = (float)(1.0 / j.fdy);
+#ifdef QEW_BOUNDS_CHECK
+    nz.oob = j.oob;
+#endif
     return nz;
 }
 
@@ -112,6 +121,7 @@ k_ensemble(const EnsJob *__restrict__ jobs, const int *__restrict__ order, int c
 extern "C" qew_status qew_ensemble_minimize(qew_ctx *ctx, int count, const qew_ensemble_line *lines,
                                             const qew_ensemble_params *ep,
                                             qew_lbfgs_result *results) {
+    QEW_RANGE();
     if (!ctx || count < 0 || (count > 0 && (!lines || !results)) || !ep)
         return qew_fail(ctx, QEW_ERR_INVALID, "ensemble_minimize: bad arguments");
     if (count == 0) return QEW_OK;
@@ -133,6 +143,9 @@ extern "C" qew_status qew_ensemble_minimize(qew_ctx *ctx, int count, const qew_e
         j.coef64 = f->coef64;
         j.poly64 = f->poly64;
         j.ky = make_bspline64(f).ky;
+#ifdef QEW_BOUNDS_CHECK
+        j.oob = qew_bounds_words();
+#endif
         j.coef32 = f->coef32;
         j.edge32 = f->edge32;
         j.nx = f->nx;
@@ -342,6 +355,9 @@ qew_status qew_lane_publish(StaticLane *L, const qew_field *f, double *d_h, int 
     j.coef64 = f->coef64;
     j.poly64 = f->poly64;
     j.ky = make_bspline64(f).ky;
+#ifdef QEW_BOUNDS_CHECK
+    j.oob = qew_bounds_words();
+#endif
     j.coef32 = f->coef32;
     j.edge32 = f->edge32;
     j.nx = f->nx;

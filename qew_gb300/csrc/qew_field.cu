@@ -324,17 +324,20 @@ extern "C" {
 
 qew_status qew_field_create_from_host(qew_ctx *ctx, const double *h_field, int nx, int ny,
                                       double Lx, double Ly, int store_flags, qew_field **out) {
+    QEW_RANGE();
     return field_build(ctx, h_field, false, nx, ny, Lx, Ly, store_flags, out);
 }
 
 qew_status qew_field_create_from_device(qew_ctx *ctx, const double *d_field, int nx, int ny,
                                         double Lx, double Ly, int store_flags, qew_field **out) {
+    QEW_RANGE();
     return field_build(ctx, d_field, true, nx, ny, Lx, Ly, store_flags, out);
 }
 
 qew_status qew_field_create_generated(qew_ctx *ctx, int nx, int ny, double Lx, double Ly,
                                      double amplitude, double xi_x_cells, double xi_y_cells,
                                      uint64_t seed, int store_flags, qew_field **out) {
+    QEW_RANGE();
     if (!ctx || !out || nx <= 0 || ny <= 0 || !(xi_x_cells >= 0) || !(xi_y_cells >= 0) ||
         xi_x_cells > 4096 || xi_y_cells > 4096 || !(amplitude > 0))
         return qew_fail(ctx, QEW_ERR_INVALID, "field_create_generated: bad arguments");
@@ -376,6 +379,7 @@ qew_status qew_field_create_generated(qew_ctx *ctx, int nx, int ny, double Lx, d
 qew_status qew_field_create_seeded(qew_ctx *ctx, int nx, int ny, double Lx, double Ly,
                                   double amplitude, double xi_x, double xi_y, uint64_t seed,
                                   int store_flags, qew_field **out) {
+    QEW_RANGE();
     if (!ctx || !out || nx <= 0 || ny <= 0 || !(Lx > 0) || !(Ly > 0) ||
         !std::isfinite(amplitude) || !std::isfinite(xi_x) || !std::isfinite(xi_y))
         return qew_fail(ctx, QEW_ERR_INVALID, "field_create_seeded: bad arguments");

@@ -111,6 +111,7 @@ qew_status qew_fire_default_params(qew_fire_params *fp) {
 qew_status qew_fire_minimize(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
                              const qew_params *p, const qew_fire_params *fp,
                              qew_fire_result *res) {
+    QEW_RANGE();
     if (!ctx || !field || !d_h || !p || !fp || !res || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "fire_minimize: bad arguments");
     if (!(fp->dt_max > 0) || fp->max_iter < 0)

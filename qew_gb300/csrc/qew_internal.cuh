@@ -19,6 +19,7 @@
 #include <string>
 
 #include "../../include/qew_gpu.h"
+#include "qew_nvtx.cuh"
 
 // ---------------------------------------------------------------- handles
 struct qew_ctx {
@@ -92,6 +93,44 @@ qew_status qew_launch_check(qew_ctx *ctx, const char *what, int k = 1);
         qew_status s__ = (expr);                                             \
         if (s__ != QEW_OK) return s__;                                       \
     } while (0)
+
+// ------------------------------------------------------ bounds-check build
+// Built with -DQEW_BOUNDS_CHECK (qew_gb300/build.py bounds_check=True), every
+// field gather and the gradient kernels' shared-memory indices are checked:
+// an index outside its array is counted in mapped host words (count, first
+// index, its bound, source line; qew_bounds_check_report reads them) and
+// clamped into range, so the access stays in bounds. The normal build
+// compiles the bare accesses: these macros discard their check arguments.
+#ifdef QEW_BOUNDS_CHECK
+// Device address of the four mapped host words (allocated on first use).
+unsigned long long *qew_bounds_words();
+__device__ __forceinline__ long long qew_bc(long long i, long long n, unsigned long long *w,
+                                            int line) {
+    if (i >= 0 && i < n) return i;
+    if (w && atomicAdd(w, 1ull) == 0ull) {
+        w[1] = (unsigned long long)i;
+        w[2] = (unsigned long long)n;
+        w[3] = (unsigned long long)line;
+    }
+    return i < 0 ? 0 : (n > 0 ? n - 1 : 0);
+}
+template <class T>
+__device__ __forceinline__ T qew_ldg_checked(const T *base, size_t off, size_t size,
+                                             unsigned long long *w, int line) {
+    return __ldg(base + (size_t)qew_bc((long long)off, (long long)size, w, line));
+}
+#define QEW_OOB_MEMBER unsigned long long *oob = nullptr;
+#define QEW_IDX(i, n, w) ((int)qew_bc((i), (n), (w), __LINE__))
+#define QEW_LDG(base, off, size, w) qew_ldg_checked((base), (off), (size), (w), __LINE__)
+#define QEW_OOB_PARAMS , size_t oob_n, unsigned long long *oob
+#define QEW_OOB_ARGS(n, w) , (n), (w)
+#else
+#define QEW_OOB_MEMBER
+#define QEW_IDX(i, n, w) (i)
+#define QEW_LDG(base, off, size, w) __ldg((base) + (off))
+#define QEW_OOB_PARAMS
+#define QEW_OOB_ARGS(n, w)
+#endif
 
 // ------------------------------------------------------------ B-spline math
 // Cubic B-spline weights for neighbours {i-1,i,i+1,i+2} at fraction t
@@ -258,6 +297,7 @@ struct NoiseBSpline64 {
     // (kPolyNotPow2 when dy is not a power of two).
     const double *__restrict__ poly;
     int ky;
+    QEW_OOB_MEMBER
 
     // Row cell and fraction of height y: from y's bits when dy is a power of
     // two and y / dy lies in [0, ny), else the reference's locate.
@@ -268,7 +308,9 @@ struct NoiseBSpline64 {
     }
 
     __device__ __forceinline__ double c(int ix, int iy) const {
-        return __ldg(coef + (size_t)iy * (size_t)nx + ix);
+        ix = QEW_IDX(ix, nx, oob);
+        iy = QEW_IDX(iy, ny, oob);
+        return QEW_LDG(coef, (size_t)iy * (size_t)nx + ix, (size_t)nx * (size_t)ny, oob);
     }
     __device__ __forceinline__ void locate(double x, double y, int ixn[4],
                                            int iyn[4], double &fx,
@@ -321,6 +363,8 @@ struct NoiseBSpline64 {
             int iy;
             double t, q0, q1, q2;
             poly_row(y, iy, t);
+            iy = QEW_IDX(iy, ny, oob);
+            e = QEW_IDX(e, nx, oob);
             poly_load3(poly + ((size_t)iy * (size_t)nx + (size_t)e) * 4, q0, q1, q2);
             return poly_dvdy(q0, q1, q2, t);
         }
@@ -346,6 +390,8 @@ struct NoiseBSpline64 {
             int iy;
             double t, q0, q1, q2, v0;
             poly_row(y, iy, t);
+            iy = QEW_IDX(iy, ny, oob);
+            e = QEW_IDX(e, nx, oob);
             poly_load4(poly + ((size_t)iy * (size_t)nx + (size_t)e) * 4, q0, q1, q2, v0);
             return poly_value(q0, q1, q2, v0, t, dy);
         }
@@ -563,6 +609,18 @@ struct NoiseSinCos {  // AnalyticNoise{amp, kx, ky}
     }
 };
 
+#ifdef QEW_BOUNDS_CHECK
+// The error words a functor carries (none for the analytic potentials).
+template <class Noise>
+__device__ __forceinline__ unsigned long long *qew_noise_oob(const Noise &) { return nullptr; }
+__device__ __forceinline__ unsigned long long *qew_noise_oob(const NoiseBSpline64 &nz) {
+    return nz.oob;
+}
+__device__ __forceinline__ unsigned long long *qew_noise_oob(const NoiseBSpline64Ref &nz) {
+    return nz.b.oob;
+}
+#endif
+
 // Edge accessors for every functor: the B-spline one has its own fast path.
 template <class Noise>
 __device__ __forceinline__ double noise_dvdy_edge(const Noise &nz, int, double xc, double y) {
@@ -615,6 +673,9 @@ static inline NoiseBSpline64 make_bspline64(const qew_field *f, int n = 0,
         const double m = frexp(f->dy, &e);  // dy = m 2^e
         nz.ky = (f->dy > 0 && m == 0.5) ? 1 - e : kPolyNotPow2;
     }
+#ifdef QEW_BOUNDS_CHECK
+    nz.oob = qew_bounds_words();
+#endif
     return nz;
 }
 

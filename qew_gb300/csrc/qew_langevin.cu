@@ -181,6 +181,7 @@ qew_status qew_langevin_destroy(qew_langevin *l) {
 
 qew_status qew_langevin_step(qew_langevin *l, const qew_field *field, double *d_h,
                              const qew_params *p, double drift, double diff) {
+    QEW_RANGE();
     QEW_TRY(check(l, field, d_h, p));
     qew_ctx *ctx = l->ctx;
     const int n = l->n;
@@ -199,6 +200,7 @@ qew_status qew_langevin_step(qew_langevin *l, const qew_field *field, double *d_
 qew_status qew_langevin_step_increments(qew_langevin *l, const qew_field *field, double *d_h,
                                         const qew_params *p, double drift, double diff,
                                         const double *d_xi) {
+    QEW_RANGE();
     QEW_TRY(check(l, field, d_h, p));
     qew_ctx *ctx = l->ctx;
     const int n = l->n;
@@ -225,6 +227,7 @@ uint64_t qew_langevin_steps(const qew_langevin *l) { return l ? l->step : 0; }
 qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h,
                             const qew_params *p, int steps, const double *h_drift,
                             const double *h_diff, int precision) {
+    QEW_RANGE();
     QEW_TRY(check(l, field, d_h, p));
     qew_ctx *ctx = l->ctx;
     if (steps < 0 || (steps > 0 && (!h_drift || !h_diff)))

@@ -309,6 +309,7 @@ qew_status qew_lbfgs_default_params(qew_lbfgs_params *lp) {
 qew_status qew_lbfgs_minimize_form(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
                                    const qew_params *p, const qew_lbfgs_params *lp, int form,
                                    qew_lbfgs_result *res) {
+    QEW_RANGE();
     if (!ctx || !field || !d_h || !p || !lp || !res || n < 1 || lp->max_ls < 0 || lp->max_iter < 0)
         return qew_fail(ctx, QEW_ERR_INVALID, "lbfgs_minimize: bad arguments");
     // The reference indexes an empty history when m == 0 (lbfgs.h:264-268).
@@ -327,6 +328,7 @@ qew_status qew_lbfgs_minimize(qew_ctx *ctx, const qew_field *field, double *d_h,
 
 qew_status qew_precond_apply(qew_ctx *ctx, const double *d_q, int n, double line_tension,
                              double physical_size, double shift, int form, double *d_out) {
+    QEW_RANGE();
     if (!ctx || !d_q || !d_out || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "precond_apply: bad arguments");
     if (form == QEW_LBFGS_PLAIN)

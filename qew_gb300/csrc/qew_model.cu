@@ -106,6 +106,7 @@ extern "C" {
 
 qew_status qew_objective(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
                          const qew_params *p, double *h_out) {
+    QEW_RANGE();
     if (!d_h) return qew_fail(ctx, QEW_ERR_INVALID, "objective: null h");
     return objective_impl(ctx, field, LineAt{d_h}, n, p, h_out);
 }
@@ -113,22 +114,26 @@ qew_status qew_objective(qew_ctx *ctx, const qew_field *field, const double *d_h
 qew_status qew_objective_trial(qew_ctx *ctx, const qew_field *field, const double *d_x0,
                                const double *d_d, double alpha, int n, const qew_params *p,
                                double *h_out) {
+    QEW_RANGE();
     if (!d_x0 || !d_d) return qew_fail(ctx, QEW_ERR_INVALID, "objective_trial: null input");
     return objective_impl(ctx, field, TrialAt{d_x0, d_d, alpha}, n, p, h_out);
 }
 
 qew_status qew_gradient(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
                         const qew_params *p, double *d_grad) {
+    QEW_RANGE();
     return qew_gradient_enqueue(ctx, field, d_h, n, p, QEW_PREC_FP64, d_grad);
 }
 
 qew_status qew_gradient_prec(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
                              const qew_params *p, int precision, double *d_grad) {
+    QEW_RANGE();
     return qew_gradient_enqueue(ctx, field, d_h, n, p, precision, d_grad);
 }
 
 qew_status qew_gradient_batch(qew_ctx *ctx, const qew_field *field, int count, const double *d_h,
                               int n, const qew_params *p, int precision, double *d_grad) {
+    QEW_RANGE();
     if (!ctx || !field || !p || !d_h || !d_grad || n < 1 || count < 0)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_batch: bad arguments");
     if (count == 0) return QEW_OK;
@@ -144,6 +149,7 @@ qew_status qew_gradient_batch(qew_ctx *ctx, const qew_field *field, int count, c
 
 qew_status qew_gradient_host(qew_ctx *ctx, const qew_field *field, const double *h_h, int n,
                              const qew_params *p, int precision, double *h_grad) {
+    QEW_RANGE();
     if (!ctx || !h_h || !h_grad || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_host: bad arguments");
     QEW_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -168,6 +174,7 @@ qew_status qew_gradient_host(qew_ctx *ctx, const qew_field *field, const double 
 qew_status qew_gradient_host_batch(qew_ctx *ctx, const qew_field *field, int count,
                                    const double *h_h, int n, const qew_params *p, int precision,
                                    double *h_grad) {
+    QEW_RANGE();
     if (!ctx || !h_h || !h_grad || n < 1 || count < 0)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_host_batch: bad arguments");
     if (count == 0) return QEW_OK;

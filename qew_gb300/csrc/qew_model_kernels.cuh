@@ -80,16 +80,22 @@ k_gradient(const double *__restrict__ h, int n, LineDx dx, double lt, double f, 
     const int i = base + t;
     const int cnt = min(BS, n - base);
     const bool arc = (model == QEW_MODEL_ARCLENGTH);
-    if (t < cnt) s_h[t + 1] = h[i];
+#ifdef QEW_BOUNDS_CHECK
+    unsigned long long *oob = qew_noise_oob(nz);
+#endif
+    if (t < cnt) s_h[QEW_IDX(t + 1, BS + 2, oob)] = h[i];
     if (t == 0) s_h[0] = h[base == 0 ? n - 1 : base - 1];
-    if (t == cnt - 1) s_h[cnt + 1] = h[(i + 1 == n) ? 0 : i + 1];
+    if (t == cnt - 1) s_h[QEW_IDX(cnt + 1, BS + 2, oob)] = h[(i + 1 == n) ? 0 : i + 1];
     __syncthreads();
-    if (t < cnt) edge_gradient(nz, i, n, s_h[t + 1], s_h[t + 2], dx, arc, s_dv[t + 1], s_sl[t + 1]);
+    if (t < cnt)
+        edge_gradient(nz, i, n, s_h[t + 1], s_h[QEW_IDX(t + 2, BS + 2, oob)], dx, arc,
+                      s_dv[QEW_IDX(t + 1, BS + 1, oob)], s_sl[t + 1]);
     if (t == 0) edge_gradient(nz, base == 0 ? n - 1 : base - 1, n, s_h[0], s_h[1], dx, arc, s_dv[0], s_sl[0]);
     __syncthreads();
     if (t < cnt)
-        grad[i] = site_gradient(s_h[t], s_h[t + 1], s_h[t + 2], s_dv[t], s_dv[t + 1], s_sl[t],
-                                s_sl[t + 1], dx, lt, f, arc);
+        grad[i] = site_gradient(s_h[t], s_h[t + 1], s_h[QEW_IDX(t + 2, BS + 2, oob)], s_dv[t],
+                                s_dv[QEW_IDX(t + 1, BS + 1, oob)], s_sl[t], s_sl[t + 1], dx, lt,
+                                f, arc);
 }
 
 // Objective with a deterministic two-level reduction: fixed grid-stride

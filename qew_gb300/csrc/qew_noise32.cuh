@@ -34,6 +34,7 @@ struct NoiseSplit32 {
     bool dx_pow2, dy_pow2;
     bool xconst;  // as NoiseBSpline64::xconst
     float inv_dy_f;
+    QEW_OOB_MEMBER
 
     __device__ __forceinline__ void loc_x(double x, int &ix, float &fx) const {
         double f;
@@ -56,12 +57,15 @@ struct NoiseSplit32 {
         if (ix >= 1 && ix <= nx - 3 && iy >= 1 && iy <= ny - 3) {
             // no wrap on either axis: one base pointer, taps at fixed offsets
             // (the same sum in the same order as below)
-            const float *p = coef + ((size_t)(iy - 1) * (size_t)nx + (size_t)(ix - 1));
+            const size_t p = (size_t)(iy - 1) * (size_t)nx + (size_t)(ix - 1);
+            const size_t N = (size_t)nx * (size_t)ny;
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
-                const float *row = p + (size_t)b * (size_t)nx;
-                const float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) +
-                                wx[2] * __ldg(row + 2) + wx[3] * __ldg(row + 3);
+                const size_t row = p + (size_t)b * (size_t)nx;
+                const float r = wx[0] * QEW_LDG(coef, row, N, oob) +
+                                wx[1] * QEW_LDG(coef, row + 1, N, oob) +
+                                wx[2] * QEW_LDG(coef, row + 2, N, oob) +
+                                wx[3] * QEW_LDG(coef, row + 3, N, oob);
                 acc += wy[b] * r;
             }
             return acc;
@@ -69,11 +73,14 @@ struct NoiseSplit32 {
         int xs[4], ys[4];
         wrap4(ix, nx, xs);
         wrap4(iy, ny, ys);
+        const size_t N = (size_t)nx * (size_t)ny;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const float *row = coef + (size_t)ys[b] * (size_t)nx;
-            const float r = wx[0] * __ldg(row + xs[0]) + wx[1] * __ldg(row + xs[1]) +
-                            wx[2] * __ldg(row + xs[2]) + wx[3] * __ldg(row + xs[3]);
+            const size_t row = (size_t)ys[b] * (size_t)nx;
+            const float r = wx[0] * QEW_LDG(coef, row + xs[0], N, oob) +
+                            wx[1] * QEW_LDG(coef, row + xs[1], N, oob) +
+                            wx[2] * QEW_LDG(coef, row + xs[2], N, oob) +
+                            wx[3] * QEW_LDG(coef, row + xs[3], N, oob);
             acc += wy[b] * r;
         }
         return acc;
@@ -86,16 +93,19 @@ struct NoiseSplit32 {
         else
             bsw_value32(fy, wy);
         float acc = 0.0f;
+        const size_t N = (size_t)nx * (size_t)ny;
         if (iy >= 1 && iy <= ny - 3) {
-            const float *p = edge + ((size_t)(iy - 1) * (size_t)nx + (size_t)e);
+            const size_t p = (size_t)(iy - 1) * (size_t)nx + (size_t)e;
 #pragma unroll
-            for (int b = 0; b < 4; ++b) acc += wy[b] * __ldg(p + (size_t)b * (size_t)nx);
+            for (int b = 0; b < 4; ++b)
+                acc += wy[b] * QEW_LDG(edge, p + (size_t)b * (size_t)nx, N, oob);
             return acc;
         }
         int ys[4];
         wrap4(iy, ny, ys);
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc += wy[b] * __ldg(edge + (size_t)ys[b] * (size_t)nx + (size_t)e);
+        for (int b = 0; b < 4; ++b)
+            acc += wy[b] * QEW_LDG(edge, (size_t)ys[b] * (size_t)nx + (size_t)e, N, oob);
         return acc;
     }
     __device__ __forceinline__ double value(double x, double y) const {
@@ -135,6 +145,11 @@ struct NoiseSplit32 {
     }
 };
 
+#ifdef QEW_BOUNDS_CHECK
+__device__ __forceinline__ unsigned long long *qew_noise_oob(const NoiseSplit32 &nz) {
+    return nz.oob;
+}
+#endif
 __device__ __forceinline__ double noise_dvdy_edge(const NoiseSplit32 &nz, int e, double xc,
                                                   double y) {
     return nz.dvdy_edge(e, xc, y);
@@ -158,5 +173,8 @@ static inline NoiseSplit32 make_split32(const qew_field *f, int n, double physic
     nz.xconst = (n > 0 && n == f->nx && physical_size == f->Lx && nz.dx_pow2);
     nz.edge = nz.xconst ? f->edge32 : nullptr;
     nz.inv_dy_f = (float)(1.0 / f->dy);
+#ifdef QEW_BOUNDS_CHECK
+    nz.oob = qew_bounds_words();
+#endif
     return nz;
 }

@@ -51,6 +51,8 @@ __device__ __forceinline__ double poly_edge_dvdy(const PolyGeom &g, int e, doubl
         int iy;
         double t;
         poly_locate(a, g.ky, g.half_inv_dy, g.nz, iy, t);
+        iy = QEW_IDX(iy, g.nz.ny, g.nz.oob);
+        e = QEW_IDX(e, g.nz.nx, g.nz.oob);
         double q0, q1, q2;
         poly_load3(g.poly + ((size_t)iy * (size_t)g.nz.nx + (size_t)e) * 4, q0, q1, q2);
         return poly_dvdy(q0, q1, q2, t);
@@ -114,6 +116,7 @@ k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ g
         __syncthreads();
         if (nline < count) fetch(nline, nidx, buf ^ 1);
         auto edge = [&](int e, int slot) {
+            slot = QEW_IDX(slot, kTile + 1, g.nz.oob);
             const double he = sh[slot], hep = sh[slot + 1];
             s_dv[slot] = poly_edge_dvdy(g, e, he, hep);
             if (kArc) {
@@ -131,8 +134,8 @@ k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ g
         double *out = grad + (size_t)line * (size_t)n + base;
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
-            const int j = t + k * kBS;
-            if (j >= cnt) break;
+            const int j = QEW_IDX(t + k * kBS, kTile, g.nz.oob);
+            if (t + k * kBS >= cnt) break;
             const double rest = fma(g.half_dx, s_dv[j] + s_dv[j + 1], -g.fdx);
             double gr;
             if (kArc) {
@@ -150,29 +153,53 @@ k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ g
 }
 
 // {q0, q1, q2, v0} of every (row cell j, column e) from the FP64
-// coefficients c ([ny][nx]); see qew_poly.cuh for the formulas.
-__global__ void k_poly_store(const double *__restrict__ c, int nx, int ny, double inv_dy,
-                             double *__restrict__ out) {
-    const double w0 = 1.0 / 48.0, w1 = 23.0 / 48.0, s6 = 1.0 / 6.0;
-    for (int j = blockIdx.y; j < ny; j += gridDim.y) {
-        int rows[4];
-        wrap4(j, ny, rows);
-        for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nx; e += gridDim.x * blockDim.x) {
-            const int em = (e == 0) ? nx - 1 : e - 1;
-            const int ep = (e + 1 == nx) ? 0 : e + 1;
-            const int ep2 = (ep + 1 == nx) ? 0 : ep + 1;
-            double E[4];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const double *r = c + (size_t)rows[b] * (size_t)nx;
-                E[b] = w0 * r[em] + w1 * r[e] + w1 * r[ep] + w0 * r[ep2];
-            }
-            double *o = out + ((size_t)j * (size_t)nx + (size_t)e) * 4;
-            o[0] = 0.5 * (E[2] - E[0]) * inv_dy;
-            o[1] = ((E[0] + E[2]) - 2.0 * E[1]) * inv_dy;
-            o[2] = 0.5 * ((E[3] - E[0]) + 3.0 * (E[1] - E[2])) * inv_dy;
-            o[3] = (E[0] + 4.0 * E[1] + E[2]) * s6;
-        }
+// coefficients c ([ny][nx]); see qew_poly.cuh for the formulas. Each thread
+// walks kStoreRows row cells of one column and filters each coefficient row
+// along x once: cell j takes the filtered values of rows j-1..j+2 from a
+// window of four, so a cell costs one x-filter (4 FP64 instructions) and the
+// combination (11) instead of four x-filters. FP64-instruction bound.
+constexpr int kStoreRows = 32;
+constexpr int kStoreBS = 256;
+
+__device__ __forceinline__ double x_filter(const double *__restrict__ r, int em, int e, int ep,
+                                           int ep2) {
+    const double w0 = 1.0 / 48.0, w1 = 23.0 / 48.0;
+    return __fma_rn(w0, __ldg(r + ep2),
+                    __fma_rn(w1, __ldg(r + ep), __fma_rn(w1, __ldg(r + e), w0 * __ldg(r + em))));
+}
+
+__global__ void __launch_bounds__(kStoreBS) k_poly_store(const double *__restrict__ c, int nx,
+                                                         int ny, double inv_dy,
+                                                         double *__restrict__ out) {
+    const int e = blockIdx.x * kStoreBS + threadIdx.x;
+    if (e >= nx) return;
+    const int j0 = blockIdx.y * kStoreRows;
+    const int j1 = min(ny, j0 + kStoreRows);
+    const int em = (e == 0) ? nx - 1 : e - 1;
+    const int ep = (e + 1 == nx) ? 0 : e + 1;
+    const int ep2 = (ep + 1 == nx) ? 0 : ep + 1;
+    const double half_inv_dy = 0.5 * inv_dy, s6 = 1.0 / 6.0;
+    int r = (j0 == 0) ? ny - 1 : j0 - 1;  // row j0-1, periodic
+    double E0 = x_filter(c + (size_t)r * nx, em, e, ep, ep2);
+    r = (r + 1 == ny) ? 0 : r + 1;
+    double E1 = x_filter(c + (size_t)r * nx, em, e, ep, ep2);
+    r = (r + 1 == ny) ? 0 : r + 1;
+    double E2 = x_filter(c + (size_t)r * nx, em, e, ep, ep2);
+    for (int j = j0; j < j1; ++j) {
+        r = (r + 1 == ny) ? 0 : r + 1;  // row j+2
+        const double E3 = x_filter(c + (size_t)r * nx, em, e, ep, ep2);
+        const double s02 = E0 + E2;
+        const double q0 = (E2 - E0) * half_inv_dy;
+        const double q1 = __fma_rn(-2.0, E1, s02) * inv_dy;
+        const double q2 = __fma_rn(3.0, E1 - E2, E3 - E0) * half_inv_dy;
+        const double v0 = __fma_rn(4.0, E1, s02) * s6;
+        double *o = out + ((size_t)j * (size_t)nx + (size_t)e) * 4;  // 32-byte aligned
+        asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(o), "d"(q0), "d"(q1),
+                     "d"(q2), "d"(v0)
+                     : "memory");
+        E0 = E1;
+        E1 = E2;
+        E2 = E3;
     }
 }
 
@@ -185,8 +212,11 @@ bool qew_poly_applies(const qew_field *f, int n, const qew_params *p) {
 
 qew_status qew_poly_store_build(qew_ctx *ctx, const double *c, int nx, int ny, double dy,
                                 double *out) {
-    const dim3 grid((unsigned)std::min((nx + 255) / 256, 64), (unsigned)std::min(ny, 65535));
-    k_poly_store<<<grid, 256, 0, ctx->stream>>>(c, nx, ny, 1.0 / dy, out);
+    if ((ny + kStoreRows - 1) / kStoreRows > 65535)
+        return qew_fail(ctx, QEW_ERR_INVALID, "poly store: more than 2^21 field rows");
+    const dim3 grid((unsigned)((nx + kStoreBS - 1) / kStoreBS),
+                    (unsigned)((ny + kStoreRows - 1) / kStoreRows));
+    k_poly_store<<<grid, kStoreBS, 0, ctx->stream>>>(c, nx, ny, 1.0 / dy, out);
     return qew_launch_check(ctx, "poly_store");
 }
 

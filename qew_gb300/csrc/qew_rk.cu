@@ -110,6 +110,7 @@ extern "C" {
 
 qew_status qew_rk_site_velocity(qew_ctx *ctx, const qew_field *field, const double *d_h, int n,
                                 const qew_params *p, double *d_vel) {
+    QEW_RANGE();
     if (!ctx || !field || !d_h || !p || !d_vel || n < 1)
         return qew_fail(ctx, QEW_ERR_INVALID, "rk_site_velocity: bad arguments");
     const double dx = p->physical_size / (double)n;
@@ -122,6 +123,7 @@ qew_status qew_rk_site_velocity(qew_ctx *ctx, const qew_field *field, const doub
 
 qew_status qew_rk_block(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
                         const qew_params *p, const qew_rk_params *rp, qew_rk_result *res) {
+    QEW_RANGE();
     if (!ctx || !field || !d_h || !res) return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: bad arguments");
     QEW_TRY(qew_rk_validate(ctx, n, p, rp));
     QEW_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -131,6 +133,7 @@ qew_status qew_rk_block(qew_ctx *ctx, const qew_field *field, double *d_h, int n
 qew_status qew_rk_block_form(qew_ctx *ctx, const qew_field *field, double *d_h, int n,
                              const qew_params *p, const qew_rk_params *rp, int form,
                              int precision, qew_rk_result *res) {
+    QEW_RANGE();
     if (!ctx || !field || !d_h || !res) return qew_fail(ctx, QEW_ERR_INVALID, "rk_block: bad arguments");
     QEW_TRY(qew_rk_validate(ctx, n, p, rp));
     QEW_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -171,6 +174,7 @@ qew_status qew_depinning_bisect_ex(qew_ctx *ctx, const qew_field *field, double 
                                    const qew_params *p, const qew_rk_params *rp, double f_lo,
                                    double f_hi, double rtol, int max_steps, int precision,
                                    qew_bisect_result *res, int *h_verdicts) {
+    QEW_RANGE();
     if (!ctx || !field || !d_h || !res || !(f_hi >= f_lo) || max_steps < 0)
         return qew_fail(ctx, QEW_ERR_INVALID, "depinning_bisect: bad arguments");
     QEW_TRY(qew_rk_validate(ctx, n, p, rp));

@@ -88,6 +88,7 @@ void qew_static_config_default(qew_static_config *c) {
 
 qew_status qew_static_sweep(qew_ctx *ctx, const qew_field *field, const qew_static_config *c,
                             qew_static_profile *profiles, double *h_out) {
+    QEW_RANGE();
     if (!ctx || !field || !c || c->nx < 1 || c->n_pinning_lengths < 0 ||
         (c->n_pinning_lengths > 0 && (!c->pinning_lengths_over_xi || !profiles || !h_out)) ||
         !model_ok(c->model))
@@ -171,6 +172,7 @@ void qew_dynamic_config_default(qew_dynamic_config *c) {
 
 qew_status qew_dynamic_anneal(qew_ctx *ctx, const qew_field *field, const qew_dynamic_config *c,
                               qew_snapshot_fn on_snapshot, void *user, qew_dynamic_result *res) {
+    QEW_RANGE();
     if (!ctx || !field || !c || !res || c->nx < 1 || !model_ok(c->model) || !(c->tau > 0) ||
         !(c->amplitude != 0) || !std::isfinite(c->total_time))
         return qew_fail(ctx, QEW_ERR_INVALID, "dynamic_anneal: bad arguments");
@@ -271,6 +273,7 @@ void qew_depinning_config_default(qew_depinning_config *c) {
 
 qew_status qew_depinning_ramp(qew_ctx *ctx, const qew_field *field, const qew_depinning_config *c,
                               qew_depinning_fn on_step, void *user, qew_depinning_result *res) {
+    QEW_RANGE();
     if (!ctx || !field || !c || !res || c->nx < 1 || !model_ok(c->model) ||
         !std::isfinite(c->f_step) || !std::isfinite(c->f_max))
         return qew_fail(ctx, QEW_ERR_INVALID, "depinning_ramp: bad arguments");

@@ -82,7 +82,7 @@ __device__ __forceinline__ void edge_x(const SplitGeom &g, int e, int &ix, float
 // wrapping around the field on either axis).
 __device__ __forceinline__
 float split_dvdy(const float *__restrict__ coef, int nx, int ny, int ix, float fx, int cy,
-                 float fy, float inv_dy) {
+                 float fy, float inv_dy QEW_OOB_PARAMS) {
     int xs[4], ys[4];
     wrap4(ix, nx, xs);
     wrap4(wrap_cell(cy, ny), ny, ys);
@@ -92,9 +92,11 @@ float split_dvdy(const float *__restrict__ coef, int nx, int ny, int ix, float f
     float dg = 0.0f;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const float *row = coef + (size_t)ys[b] * (size_t)nx;
-        const float r = wx[0] * __ldg(row + xs[0]) + wx[1] * __ldg(row + xs[1]) +
-                        wx[2] * __ldg(row + xs[2]) + wx[3] * __ldg(row + xs[3]);
+        const size_t row = (size_t)ys[b] * (size_t)nx;
+        const float r = wx[0] * QEW_LDG(coef, row + xs[0], oob_n, oob) +
+                        wx[1] * QEW_LDG(coef, row + xs[1], oob_n, oob) +
+                        wx[2] * QEW_LDG(coef, row + xs[2], oob_n, oob) +
+                        wx[3] * QEW_LDG(coef, row + xs[3], oob_n, oob);
         dg += dwy[b] * r;
     }
     return dg * inv_dy;
@@ -106,16 +108,18 @@ float split_dvdy(const float *__restrict__ coef, int nx, int ny, int ix, float f
 // same order as split_dvdy, so the result is identical.
 __device__ __forceinline__ float split_dvdy_interior(const float *__restrict__ coef, int nx,
                                                      int ix, const float wx[4], int cy, float fy,
-                                                     float inv_dy) {
+                                                     float inv_dy QEW_OOB_PARAMS) {
     float dwy[4];
     bsw_deriv_f(fy, dwy);
-    const float *p = coef + ((size_t)(cy - 1) * (size_t)nx + (size_t)(ix - 1));
+    const size_t p = (size_t)(cy - 1) * (size_t)nx + (size_t)(ix - 1);
     float dg = 0.0f;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const float *row = p + (size_t)b * (size_t)nx;
-        const float r = wx[0] * __ldg(row) + wx[1] * __ldg(row + 1) + wx[2] * __ldg(row + 2) +
-                        wx[3] * __ldg(row + 3);
+        const size_t row = p + (size_t)b * (size_t)nx;
+        const float r = wx[0] * QEW_LDG(coef, row, oob_n, oob) +
+                        wx[1] * QEW_LDG(coef, row + 1, oob_n, oob) +
+                        wx[2] * QEW_LDG(coef, row + 2, oob_n, oob) +
+                        wx[3] * QEW_LDG(coef, row + 3, oob_n, oob);
         dg += dwy[b] * r;
     }
     return dg * inv_dy;
@@ -126,24 +130,27 @@ __device__ __forceinline__ float split_dvdy_interior(const float *__restrict__ c
 // stencil rows, one tap each. The interior form (1 <= cy <= ny - 3) indexes
 // from one base pointer; the other wraps the rows.
 __device__ __forceinline__ float split_dvdy_edge_interior(const float *__restrict__ E, int nx,
-                                                          int e, int cy, float fy, float inv_dy) {
+                                                          int e, int cy, float fy,
+                                                          float inv_dy QEW_OOB_PARAMS) {
     float dwy[4];
     bsw_deriv_f(fy, dwy);
-    const float *p = E + ((size_t)(cy - 1) * (size_t)nx + (size_t)e);
+    const size_t p = (size_t)(cy - 1) * (size_t)nx + (size_t)e;
     float dg = 0.0f;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) dg += dwy[b] * __ldg(p + (size_t)b * (size_t)nx);
+    for (int b = 0; b < 4; ++b) dg += dwy[b] * QEW_LDG(E, p + (size_t)b * (size_t)nx, oob_n, oob);
     return dg * inv_dy;
 }
 __device__ __forceinline__ float split_dvdy_edge(const float *__restrict__ E, int nx, int ny,
-                                                 int e, int cy, float fy, float inv_dy) {
+                                                 int e, int cy, float fy,
+                                                 float inv_dy QEW_OOB_PARAMS) {
     int ys[4];
     wrap4(wrap_cell(cy, ny), ny, ys);
     float dwy[4];
     bsw_deriv_f(fy, dwy);
     float dg = 0.0f;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) dg += dwy[b] * __ldg(E + (size_t)ys[b] * (size_t)nx + (size_t)e);
+    for (int b = 0; b < 4; ++b)
+        dg += dwy[b] * QEW_LDG(E, (size_t)ys[b] * (size_t)nx + (size_t)e, oob_n, oob);
     return dg * inv_dy;
 }
 
@@ -170,11 +177,16 @@ __device__ __forceinline__ void split_edge(const SplitGeom &g, const float wx_ha
                                            float *sl) {
     int cm;
     float fm;
+#ifdef QEW_BOUNDS_CHECK
+    const size_t oob_n = (size_t)g.nx * (size_t)g.ny;
+#endif
     split_mid(sc[slot], sf[slot], sc[slot + 1], sf[slot + 1], cm, fm);
     const bool y_inner = (cm >= 1 && cm <= g.ny - 3);
     if ((kStore || g.edge) && e + 1 < g.n) {  // x-filtered store: 4 taps (the wrap edge sits at (n-1)/2)
-        dv[slot] = y_inner ? split_dvdy_edge_interior(g.edge, g.nx, e, cm, fm, g.inv_dy_f)
-                           : split_dvdy_edge(g.edge, g.nx, g.ny, e, cm, fm, g.inv_dy_f);
+        dv[slot] = y_inner ? split_dvdy_edge_interior(g.edge, g.nx, e, cm, fm, g.inv_dy_f
+                                                      QEW_OOB_ARGS(oob_n, g.oob))
+                           : split_dvdy_edge(g.edge, g.nx, g.ny, e, cm, fm, g.inv_dy_f
+                                             QEW_OOB_ARGS(oob_n, g.oob));
     } else {
         int ix;
         float fx;
@@ -187,9 +199,11 @@ __device__ __forceinline__ void split_edge(const SplitGeom &g, const float wx_ha
             } else {
                 bsw_value_f(fx, wx);
             }
-            dv[slot] = split_dvdy_interior(g.coef, g.nx, ix, wx, cm, fm, g.inv_dy_f);
+            dv[slot] = split_dvdy_interior(g.coef, g.nx, ix, wx, cm, fm, g.inv_dy_f
+                                           QEW_OOB_ARGS(oob_n, g.oob));
         } else {
-            dv[slot] = split_dvdy(g.coef, g.nx, g.ny, ix, fx, cm, fm, g.inv_dy_f);
+            dv[slot] = split_dvdy(g.coef, g.nx, g.ny, ix, fx, cm, fm, g.inv_dy_f
+                                  QEW_OOB_ARGS(oob_n, g.oob));
         }
     }
     if (g.arc) {
@@ -420,6 +434,9 @@ SplitGeom qew_split_geom(const qew_field *f, int n, const qew_params *p) {
     g.dx_f = (float)dx;
     g.f = (float)p->driving_force;
     g.arc = (p->model == QEW_MODEL_ARCLENGTH) ? 1 : 0;
+#ifdef QEW_BOUNDS_CHECK
+    g.oob = qew_bounds_words();
+#endif
     return g;
 }
 
@@ -484,6 +501,7 @@ extern "C" {
 
 qew_status qew_split_heights(qew_ctx *ctx, const qew_field *f, const double *d_h, int n,
                              int32_t *d_cell, float *d_frac) {
+    QEW_RANGE();
     if (!ctx || !f || !d_h || !d_cell || !d_frac || n < 1 || f->kind != QEW_FIELD_BSPLINE)
         return qew_fail(ctx, QEW_ERR_INVALID, "split_heights: bad arguments");
     k_split_heights<<<(n + 255) / 256, 256, 0, ctx->stream>>>(
@@ -493,6 +511,7 @@ qew_status qew_split_heights(qew_ctx *ctx, const qew_field *f, const double *d_h
 
 qew_status qew_join_heights(qew_ctx *ctx, const qew_field *f, const int32_t *d_cell,
                             const float *d_frac, int n, double *d_h) {
+    QEW_RANGE();
     if (!ctx || !f || !d_h || !d_cell || !d_frac || n < 1 || f->kind != QEW_FIELD_BSPLINE)
         return qew_fail(ctx, QEW_ERR_INVALID, "join_heights: bad arguments");
     k_join_heights<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d_cell, d_frac, n, f->dy, d_h);
@@ -501,6 +520,7 @@ qew_status qew_join_heights(qew_ctx *ctx, const qew_field *f, const int32_t *d_c
 
 qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *f, const int32_t *d_cell,
                               const float *d_frac, int n, const qew_params *p, float *d_grad) {
+    QEW_RANGE();
     QEW_TRY(split_check(ctx, f, n, p));
     if (!d_cell || !d_frac || !d_grad)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split: null buffer");
@@ -510,6 +530,7 @@ qew_status qew_gradient_split(qew_ctx *ctx, const qew_field *f, const int32_t *d
 qew_status qew_gradient_split_batch(qew_ctx *ctx, const qew_field *f, int count,
                                     const int32_t *d_cell, const float *d_frac, int n,
                                     const qew_params *p, float *d_grad) {
+    QEW_RANGE();
     QEW_TRY(split_check(ctx, f, n, p));
     if (!d_cell || !d_frac || !d_grad || count < 1 || count > 65535)
         return qew_fail(ctx, QEW_ERR_INVALID, "gradient_split_batch: bad arguments");

@@ -18,6 +18,7 @@ struct SplitGeom {
     float dx_f;
     float f;
     int arc;
+    QEW_OOB_MEMBER
 };
 
 SplitGeom qew_split_geom(const qew_field *f, int n, const qew_params *p);

@@ -32,6 +32,22 @@ def test_precond_matches_oracle(Q, O, form, n):
 
 
 @pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("n", [65536, 262144])
+def test_precond_long_lines_small_shift(Q, O, form, n):
+    """Lines as long as serving's static requests and the reference's
+    benchmark, with the shifts 0.5/xi^2 of xi = 2..8 cells and smaller: the
+    periodic solve against the oracle's FFT form. The bar grows with the
+    solve's condition number (about 4 kappa/dx^2 / shift)."""
+    q = np.random.default_rng(n + 1).standard_normal(n)
+    for shift in (0.125, 0.0078125, 1e-4):
+        d = npy(Q.precond_apply(t64(q), 1.0, float(n), shift, form=form))
+        ref = O.precond_apply(q, 1.0, float(n), shift)
+        bar = 1e-13 * (4.0 / shift)
+        err = np.max(np.abs(d - ref)) / np.max(np.abs(ref))
+        assert err <= bar, (shift, err)
+
+
+@pytest.mark.parametrize("form", FORMS)
 def test_golden_minimum(Q, O, lbfgs_golden, form):
     """test_lbfgs.cpp:309-349 on the GPU, and the oracle's trajectory."""
     g = lbfgs_golden
