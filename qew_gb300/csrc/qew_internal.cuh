@@ -101,6 +101,8 @@ qew_status qew_launch_check(qew_ctx *ctx, const char *what, int k = 1);
 // index, its bound, source line; qew_bounds_check_report reads them) and
 // clamped into range, so the access stays in bounds. The normal build
 // compiles the bare accesses: these macros discard their check arguments.
+// QEW_LDGP takes the pointer itself (the normal build's address arithmetic
+// is then the unchecked code's, register for register) and the array's base.
 #ifdef QEW_BOUNDS_CHECK
 // Device address of the four mapped host words (allocated on first use).
 unsigned long long *qew_bounds_words();
@@ -121,13 +123,14 @@ __device__ __forceinline__ T qew_ldg_checked(const T *base, size_t off, size_t s
 }
 #define QEW_OOB_MEMBER unsigned long long *oob = nullptr;
 #define QEW_IDX(i, n, w) ((int)qew_bc((i), (n), (w), __LINE__))
-#define QEW_LDG(base, off, size, w) qew_ldg_checked((base), (off), (size), (w), __LINE__)
+#define QEW_LDGP(ptr, base, size, w) \
+    qew_ldg_checked((base), (size_t)((ptr) - (base)), (size), (w), __LINE__)
 #define QEW_OOB_PARAMS , size_t oob_n, unsigned long long *oob
 #define QEW_OOB_ARGS(n, w) , (n), (w)
 #else
 #define QEW_OOB_MEMBER
 #define QEW_IDX(i, n, w) (i)
-#define QEW_LDG(base, off, size, w) __ldg((base) + (off))
+#define QEW_LDGP(ptr, base, size, w) __ldg(ptr)
 #define QEW_OOB_PARAMS
 #define QEW_OOB_ARGS(n, w)
 #endif
@@ -310,7 +313,7 @@ struct NoiseBSpline64 {
     __device__ __forceinline__ double c(int ix, int iy) const {
         ix = QEW_IDX(ix, nx, oob);
         iy = QEW_IDX(iy, ny, oob);
-        return QEW_LDG(coef, (size_t)iy * (size_t)nx + ix, (size_t)nx * (size_t)ny, oob);
+        return QEW_LDGP(coef + (size_t)iy * (size_t)nx + ix, coef, (size_t)nx * (size_t)ny, oob);
     }
     __device__ __forceinline__ void locate(double x, double y, int ixn[4],
                                            int iyn[4], double &fx,

@@ -57,15 +57,14 @@ struct NoiseSplit32 {
         if (ix >= 1 && ix <= nx - 3 && iy >= 1 && iy <= ny - 3) {
             // no wrap on either axis: one base pointer, taps at fixed offsets
             // (the same sum in the same order as below)
-            const size_t p = (size_t)(iy - 1) * (size_t)nx + (size_t)(ix - 1);
-            const size_t N = (size_t)nx * (size_t)ny;
+            const float *p = coef + ((size_t)(iy - 1) * (size_t)nx + (size_t)(ix - 1));
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
-                const size_t row = p + (size_t)b * (size_t)nx;
-                const float r = wx[0] * QEW_LDG(coef, row, N, oob) +
-                                wx[1] * QEW_LDG(coef, row + 1, N, oob) +
-                                wx[2] * QEW_LDG(coef, row + 2, N, oob) +
-                                wx[3] * QEW_LDG(coef, row + 3, N, oob);
+                const float *row = p + (size_t)b * (size_t)nx;
+                const float r = wx[0] * QEW_LDGP(row, coef, (size_t)nx * ny, oob) +
+                                wx[1] * QEW_LDGP(row + 1, coef, (size_t)nx * ny, oob) +
+                                wx[2] * QEW_LDGP(row + 2, coef, (size_t)nx * ny, oob) +
+                                wx[3] * QEW_LDGP(row + 3, coef, (size_t)nx * ny, oob);
                 acc += wy[b] * r;
             }
             return acc;
@@ -73,14 +72,13 @@ struct NoiseSplit32 {
         int xs[4], ys[4];
         wrap4(ix, nx, xs);
         wrap4(iy, ny, ys);
-        const size_t N = (size_t)nx * (size_t)ny;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
-            const size_t row = (size_t)ys[b] * (size_t)nx;
-            const float r = wx[0] * QEW_LDG(coef, row + xs[0], N, oob) +
-                            wx[1] * QEW_LDG(coef, row + xs[1], N, oob) +
-                            wx[2] * QEW_LDG(coef, row + xs[2], N, oob) +
-                            wx[3] * QEW_LDG(coef, row + xs[3], N, oob);
+            const float *row = coef + (size_t)ys[b] * (size_t)nx;
+            const float r = wx[0] * QEW_LDGP(row + xs[0], coef, (size_t)nx * ny, oob) +
+                            wx[1] * QEW_LDGP(row + xs[1], coef, (size_t)nx * ny, oob) +
+                            wx[2] * QEW_LDGP(row + xs[2], coef, (size_t)nx * ny, oob) +
+                            wx[3] * QEW_LDGP(row + xs[3], coef, (size_t)nx * ny, oob);
             acc += wy[b] * r;
         }
         return acc;
@@ -93,19 +91,19 @@ struct NoiseSplit32 {
         else
             bsw_value32(fy, wy);
         float acc = 0.0f;
-        const size_t N = (size_t)nx * (size_t)ny;
         if (iy >= 1 && iy <= ny - 3) {
-            const size_t p = (size_t)(iy - 1) * (size_t)nx + (size_t)e;
+            const float *p = edge + ((size_t)(iy - 1) * (size_t)nx + (size_t)e);
 #pragma unroll
             for (int b = 0; b < 4; ++b)
-                acc += wy[b] * QEW_LDG(edge, p + (size_t)b * (size_t)nx, N, oob);
+                acc += wy[b] * QEW_LDGP(p + (size_t)b * (size_t)nx, edge, (size_t)nx * ny, oob);
             return acc;
         }
         int ys[4];
         wrap4(iy, ny, ys);
 #pragma unroll
         for (int b = 0; b < 4; ++b)
-            acc += wy[b] * QEW_LDG(edge, (size_t)ys[b] * (size_t)nx + (size_t)e, N, oob);
+            acc += wy[b] * QEW_LDGP(edge + (size_t)ys[b] * (size_t)nx + (size_t)e, edge,
+                                    (size_t)nx * ny, oob);
         return acc;
     }
     __device__ __forceinline__ double value(double x, double y) const {

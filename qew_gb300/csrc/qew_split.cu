@@ -92,11 +92,11 @@ float split_dvdy(const float *__restrict__ coef, int nx, int ny, int ix, float f
     float dg = 0.0f;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const size_t row = (size_t)ys[b] * (size_t)nx;
-        const float r = wx[0] * QEW_LDG(coef, row + xs[0], oob_n, oob) +
-                        wx[1] * QEW_LDG(coef, row + xs[1], oob_n, oob) +
-                        wx[2] * QEW_LDG(coef, row + xs[2], oob_n, oob) +
-                        wx[3] * QEW_LDG(coef, row + xs[3], oob_n, oob);
+        const float *row = coef + (size_t)ys[b] * (size_t)nx;
+        const float r = wx[0] * QEW_LDGP(row + xs[0], coef, oob_n, oob) +
+                        wx[1] * QEW_LDGP(row + xs[1], coef, oob_n, oob) +
+                        wx[2] * QEW_LDGP(row + xs[2], coef, oob_n, oob) +
+                        wx[3] * QEW_LDGP(row + xs[3], coef, oob_n, oob);
         dg += dwy[b] * r;
     }
     return dg * inv_dy;
@@ -111,15 +111,15 @@ __device__ __forceinline__ float split_dvdy_interior(const float *__restrict__ c
                                                      float inv_dy QEW_OOB_PARAMS) {
     float dwy[4];
     bsw_deriv_f(fy, dwy);
-    const size_t p = (size_t)(cy - 1) * (size_t)nx + (size_t)(ix - 1);
+    const float *p = coef + ((size_t)(cy - 1) * (size_t)nx + (size_t)(ix - 1));
     float dg = 0.0f;
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-        const size_t row = p + (size_t)b * (size_t)nx;
-        const float r = wx[0] * QEW_LDG(coef, row, oob_n, oob) +
-                        wx[1] * QEW_LDG(coef, row + 1, oob_n, oob) +
-                        wx[2] * QEW_LDG(coef, row + 2, oob_n, oob) +
-                        wx[3] * QEW_LDG(coef, row + 3, oob_n, oob);
+        const float *row = p + (size_t)b * (size_t)nx;
+        const float r = wx[0] * QEW_LDGP(row, coef, oob_n, oob) +
+                        wx[1] * QEW_LDGP(row + 1, coef, oob_n, oob) +
+                        wx[2] * QEW_LDGP(row + 2, coef, oob_n, oob) +
+                        wx[3] * QEW_LDGP(row + 3, coef, oob_n, oob);
         dg += dwy[b] * r;
     }
     return dg * inv_dy;
@@ -134,10 +134,10 @@ __device__ __forceinline__ float split_dvdy_edge_interior(const float *__restric
                                                           float inv_dy QEW_OOB_PARAMS) {
     float dwy[4];
     bsw_deriv_f(fy, dwy);
-    const size_t p = (size_t)(cy - 1) * (size_t)nx + (size_t)e;
+    const float *p = E + ((size_t)(cy - 1) * (size_t)nx + (size_t)e);
     float dg = 0.0f;
 #pragma unroll
-    for (int b = 0; b < 4; ++b) dg += dwy[b] * QEW_LDG(E, p + (size_t)b * (size_t)nx, oob_n, oob);
+    for (int b = 0; b < 4; ++b) dg += dwy[b] * QEW_LDGP(p + (size_t)b * (size_t)nx, E, oob_n, oob);
     return dg * inv_dy;
 }
 __device__ __forceinline__ float split_dvdy_edge(const float *__restrict__ E, int nx, int ny,
@@ -150,7 +150,7 @@ __device__ __forceinline__ float split_dvdy_edge(const float *__restrict__ E, in
     float dg = 0.0f;
 #pragma unroll
     for (int b = 0; b < 4; ++b)
-        dg += dwy[b] * QEW_LDG(E, (size_t)ys[b] * (size_t)nx + (size_t)e, oob_n, oob);
+        dg += dwy[b] * QEW_LDGP(E + (size_t)ys[b] * (size_t)nx + (size_t)e, E, oob_n, oob);
     return dg * inv_dy;
 }
 
