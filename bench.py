@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ensemble-lines", type=int, default=4096,
                     help="lines of the batched-statics section (0 skips it)")
+    ap.add_argument("--ensemble-store", default="fp64", choices=["fp64", "poly"],
+                    help="the ensemble fields' FP64 store: coefficients only (16 taps per "
+                         "edge), or with the cell polynomials the FP64 refinement then reads")
     ap.add_argument("--ensemble-ref", type=int, default=16,
                     help="lines timed with the plain one-line-per-launch form")
     ap.add_argument("--sections", default="refshape,static,ensemble,dynamics,depinning,serving",
@@ -393,6 +396,8 @@ def run_ensemble(args, Q, torch):
     rng = np.random.default_rng(3)
     n_lines = args.ensemble_lines
     store = Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32
+    if args.ensemble_store == "poly":
+        store |= Q.QEW_STORE_FP64_POLY
     specs, lines = [], []
     for k in range(n_lines):
         L = int(round(np.exp(rng.uniform(np.log(256), np.log(16384))) / 2)) * 2
@@ -439,6 +444,10 @@ def run_ensemble(args, Q, torch):
             "gpu_launches": launches,
             "workload": "L log-uniform [256,16384], 256-row fields, xi~U[2,8], h0=0, m=10, "
                         "preconditioned, FP32 phase to 2e-5 then FP64 to 1e-8",
+            "field_store": ("FP64 coefficients + FP32 (16 FP64 taps per edge in the refinement)"
+                            if args.ensemble_store == "fp64" else
+                            "FP64 coefficients + cell polynomials + FP32 (the refinement reads "
+                            "one 32-byte cell per edge)"),
             "plain_fp64_one_line_per_launch": {
                 "value": plain_rate, "unit": "solves/s", "sample_lines": int(len(sample)),
                 "converged": conv_plain, "verified_max_grad": gmax_plain,

@@ -59,6 +59,33 @@ def test_gradient_candidates_bitwise_equal(Q):
     assert "k_gradient_poly" in rep and "k_gradient_split_persist" in rep
 
 
+def test_gradient_candidates_on_special_heights(Q):
+    """Every launch shape of the store gather, bitwise, on heights that take
+    its exceptional paths: zeros of both signs, opposite signs (cancelling
+    midpoint sums), subnormals, exact negatives of a neighbour, values far
+    outside the field, and ties of the rounding."""
+    import torch
+    nx, ny = 4096, 32
+    f = Q.FilteredNoise(gaussian_field(nx, ny, 3.0, 8), float(nx), float(ny),
+                        store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY)
+    ctx = f.ctx
+    rng = np.random.default_rng(4)
+    h = rng.uniform(-ny, 2 * ny, nx)
+    h[0:64:2] = 0.0
+    h[1:64:2] = -0.0
+    h[64:128] = rng.choice([5e-324, 1e-310, -1e-310, 2.2250738585072014e-308], 64)
+    h[129:256:2] = -h[128:255:2]                              # a + b == 0 exactly
+    h[256:512] = np.round(h[256:512] * 2 ** 20) / 2 ** 20      # short mantissas: exact sums
+    h[512:520] = [1.0, 2.0 ** -53, 1.0, 3 * 2.0 ** -53, 1e12, -1e12, 1e6, -1e6]
+    ht = t64(h).reshape(1, nx)
+    for model in (0, 1):
+        p = Q.Params(float(nx), 1.3, 0.1, Q.Model(model))
+        outs = _each_candidate(ctx, Q.QEW_TUNE_GRADIENT_POLY, 9,
+                               lambda: Q.gradient_batch(ht, p, f).clone())
+        for c, o in enumerate(outs[1:], 1):  # bit patterns (a NaN equals itself)
+            assert torch.equal(o.view(torch.int64), outs[0].view(torch.int64)), c
+
+
 @pytest.mark.parametrize("n", [512, 8192])
 def test_rk_search_candidates_bitwise_equal(Q, n):
     import torch
