@@ -67,7 +67,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ensemble-lines", type=int, default=4096,
                     help="lines of the batched-statics section (0 skips it)")
-    ap.add_argument("--ensemble-store", default="fp64", choices=["fp64", "poly"],
+    ap.add_argument("--ensemble-store", default="poly", choices=["fp64", "poly"],
                     help="the ensemble fields' FP64 store: coefficients only (16 taps per "
                          "edge), or with the cell polynomials the FP64 refinement then reads")
     ap.add_argument("--ensemble-ref", type=int, default=16,
@@ -832,7 +832,9 @@ def fp64_peak(Q, ctx):
 # smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of one
 # launch divided by its points. For k_gradient these counters leave out its
 # FP64 floor, conversions and compares, so its fraction reads low.
-FP64_INST_PER_POINT = {"k_gradient_poly": 8.0, "k_gradient": 49.15}
+# k_gradient_poly: 7 on the headline's lines (f = 0, dx = 1: the zero-force
+# form, 4 DFMA + 3 DADD); 8 at f != 0.
+FP64_INST_PER_POINT = {"k_gradient_poly": 7.0, "k_gradient": 49.15}
 
 
 def run_sections_only(args, Q, torch, rank):

@@ -13,6 +13,13 @@
 // h_e + h_{e+1} when the row spacing is a power of two (qew_poly.cuh), so an
 // edge of the linear model costs 3 FP64 instructions and a site 5.
 //
+// At f = 0 with dx/2 a power of two 2^k (kF0) the combine's first term is an
+// exact scaling: (dx/2)(dv_{i-1} + dv_i) == dv'_{i-1} + dv'_i bit for bit
+// with dv' = 2^k dv, and each edge forms dv' by adding k to the exponent
+// field of dv (integer instructions; the FP64 multiply where dv or dv' is
+// zero, subnormal or non-finite). A site then costs 4 FP64 instructions
+// instead of 5.
+//
 // Launch: persistent, batched (lines stored n apart), one CTA per resident
 // slot; each CTA walks tiles of kTile sites gridDim.x apart and copies the
 // next tile's heights into its spare shared buffer with cp.async while the
@@ -41,7 +48,23 @@ struct PolyGeom {
     double c_el;          // -Gamma / dx
     double lt;            // Gamma
     double half_dx, fdx;  // dx / 2, dx f
+    int half_dx_exp;      // k with dx / 2 == 2^k (the kF0 form)
 };
+
+// v * scale for a zero, subnormal or non-finite v or result: a call of its
+// own, so the compiler cannot evaluate the multiply for every lane and
+// select (which would put the FP64 instruction back on every edge).
+__device__ __noinline__ double scale_pow2_slow(double v, double scale) { return v * scale; }
+
+// v * 2^k (scale == 2^k), exact: the exponent field moves by k when v and
+// the result are normal.
+__device__ __forceinline__ double scale_pow2(double v, int k, double scale) {
+    const int hi = __double2hiint(v);
+    const int e = (hi >> 20) & 0x7FF;
+    if (e != 0 && e + k >= 1 && e + k <= 2046)
+        return __hiloint2double(hi + (k << 20), __double2loint(v));
+    return scale_pow2_slow(v, scale);
+}
 
 // dV/dy at the midpoint of edge (e, e + 1 mod n) of heights he, hep.
 __device__ __forceinline__ double poly_edge_dvdy(const PolyGeom &g, int e, double he,
@@ -67,7 +90,7 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
-template <bool kArc, int kItems>
+template <bool kArc, int kItems, bool kF0>
 __global__ void __launch_bounds__(kBS, kMinCtas)
 k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ grad, int count) {
     constexpr int kTile = kBS * kItems;
@@ -118,7 +141,8 @@ k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ g
         auto edge = [&](int e, int slot) {
             slot = QEW_IDX(slot, kTile + 1, g.nz.oob);
             const double he = sh[slot], hep = sh[slot + 1];
-            s_dv[slot] = poly_edge_dvdy(g, e, he, hep);
+            const double dv = poly_edge_dvdy(g, e, he, hep);
+            s_dv[slot] = kF0 ? scale_pow2(dv, g.half_dx_exp, g.half_dx) : dv;
             if (kArc) {
                 const double dh = g.L.div(hep - he);
                 s_sl[slot] = dh * rsqrt(1.0 + dh * dh);
@@ -136,7 +160,8 @@ k_gradient_poly(const double *__restrict__ h, PolyGeom g, double *__restrict__ g
         for (int k = 0; k < kItems; ++k) {
             const int j = QEW_IDX(t + k * kBS, kTile, g.nz.oob);
             if (t + k * kBS >= cnt) break;
-            const double rest = fma(g.half_dx, s_dv[j] + s_dv[j + 1], -g.fdx);
+            const double rest = kF0 ? s_dv[j] + s_dv[j + 1]
+                                    : fma(g.half_dx, s_dv[j] + s_dv[j + 1], -g.fdx);
             double gr;
             if (kArc) {
                 gr = fma(g.lt, s_sl[j] - s_sl[j + 1], rest);
@@ -235,6 +260,9 @@ qew_status qew_gradient_poly_enqueue(qew_ctx *ctx, const qew_field *f, int count
     g.lt = p->line_tension;
     g.half_dx = 0.5 * g.L.dx;
     g.fdx = g.L.dx * p->driving_force;
+    int hx;
+    const bool f0 = p->driving_force == 0.0 && frexp(g.half_dx, &hx) == 0.5;
+    g.half_dx_exp = hx - 1;  // half_dx == 2^(hx-1) when f0
     const bool arc = (p->model == QEW_MODEL_ARCLENGTH);
     // Candidates: sites per thread {1, 2, 4} x resident CTAs per SM {2, 3, 4};
     // every one computes the same numbers (the per-site arithmetic does not
@@ -251,23 +279,25 @@ qew_status qew_gradient_poly_enqueue(qew_ctx *ctx, const qew_field *f, int count
         if (tiles > INT_MAX)
             return qew_fail(ctx, QEW_ERR_INVALID, "gradient: more than 2^31 tiles");
         const int grid = (int)std::min<long long>(tiles, (long long)ctas * ctx->num_sms);
-#define QEW_POLY_LAUNCH(A, I) \
-    k_gradient_poly<A, I><<<grid, kBS, 0, ctx->stream>>>(d_h, g, d_grad, count)
+#define QEW_POLY_LAUNCH(A, I, F) \
+    k_gradient_poly<A, I, F><<<grid, kBS, 0, ctx->stream>>>(d_h, g, d_grad, count)
+#define QEW_POLY_ITEMS(A, F)                       \
+    if (items == 1) QEW_POLY_LAUNCH(A, 1, F);      \
+    else if (items == 2) QEW_POLY_LAUNCH(A, 2, F); \
+    else QEW_POLY_LAUNCH(A, 4, F)
         if (arc) {
-            if (items == 1) QEW_POLY_LAUNCH(true, 1);
-            else if (items == 2) QEW_POLY_LAUNCH(true, 2);
-            else QEW_POLY_LAUNCH(true, 4);
+            if (f0) { QEW_POLY_ITEMS(true, true); } else { QEW_POLY_ITEMS(true, false); }
         } else {
-            if (items == 1) QEW_POLY_LAUNCH(false, 1);
-            else if (items == 2) QEW_POLY_LAUNCH(false, 2);
-            else QEW_POLY_LAUNCH(false, 4);
+            if (f0) { QEW_POLY_ITEMS(false, true); } else { QEW_POLY_ITEMS(false, false); }
         }
+#undef QEW_POLY_ITEMS
 #undef QEW_POLY_LAUNCH
         return qew_launch_check(ctx, "gradient_poly");
     };
     int cand = 5;
     QEW_TRY(qew_tune_pick(ctx, kTuneGradientPoly,
-                          qew_tune_class((long long)n * count, arc ? 1 : 0), 9, 5, names, launch,
+                          qew_tune_class((long long)n * count, (arc ? 1 : 0) + (f0 ? 2 : 0)), 9,
+                          5, names, launch,
                           &cand));
     return launch(cand);
 }

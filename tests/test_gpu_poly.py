@@ -61,6 +61,35 @@ def test_poly_gradient_matches_oracle(Q, O, model, shape):
     close(gr, go)
 
 
+@pytest.mark.parametrize("model", [0, 1])
+@pytest.mark.parametrize("scale", [1.0, 0.25, 3.0])
+def test_poly_zero_force_form_is_the_general_form(Q, O, model, scale):
+    """At f = 0 with dx/2 a power of two the store gather forms (dx/2) dv on
+    each edge by moving dv's exponent; the gradient equals, bit for bit, the
+    general form's at a force too small to change any sum (1e-300): with
+    dx/2 = 2^k the general combine fma(dx/2, S, -dx f) is an exact scaling
+    plus a negligible term. Both match the oracle at f = 0 to the bar. (At
+    dx = 3 the general form runs at f = 0 as well; there the product 1.5 S
+    is not exact, so the tiny force may tip a rounding tie and only the
+    oracle bar applies.)"""
+    import torch
+    nx, ny = 3000, 40
+    Lx = nx * scale
+    fld = gaussian_field(nx, ny, 3.0, 31)
+    f = poly_field(Q, fld, Lx, float(ny))
+    of = O.BSplineField(fld, Lx, float(ny), coef=f.coefficients())
+    rng = np.random.default_rng(model + 11)
+    h = ny / 2 + np.cumsum(rng.standard_normal(nx)) * 0.4
+    h -= np.linspace(0, h[-1] - h[0], nx)
+    h[:8] = [0.0, -0.0, 1e-310, 2.0, 2.0, -3.5, 1e6, 0.5]
+    hb = t64(np.stack([h, h[::-1].copy()]))
+    g0 = Q.gradient_batch(hb, Q.Params(Lx, 1.2, 0.0, Q.Model(model)), f)
+    gt = Q.gradient_batch(hb, Q.Params(Lx, 1.2, 1e-300, Q.Model(model)), f)
+    if scale != 3.0:
+        assert torch.equal(g0.view(torch.int64), gt.view(torch.int64))
+    close(npy(g0[0]), O.gradient(h, O.params(Lx, 1.2, 0.0, model), of))
+
+
 def test_poly_cell_boundaries_and_special_heights(Q, O):
     """Heights on exact cell boundaries, zero, tiny and negative values, and
     far outside the field: the bit-level floor/fraction agrees with the
