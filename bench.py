@@ -1011,6 +1011,15 @@ def run_ours(args):
         results[name] = {"value": val, "unit": UNIT, "ms_per_step": ms / args.steps,
                          "dtype": dt, "roofline": roof,
                          "fp64_roofline": fp64_roofline(val / max(ws, 1), kern)}
+    # The split form's API takes heights already split into (int32 cell,
+    # FP32 fraction) and returns FP32 gradients; the split of the FP64 heights
+    # is timed on its own here (one qew_split_heights call per line).
+    ms_split, _ = timed(torch, lambda: [Q.split_heights(H[k], noise) for k in range(n_inst)],
+                        args.steps, ctx)
+    results["fp32split"]["timed_region"] = (
+        "qew_gradient_split_batch on (cell, fraction) heights; the FP64 -> (cell, fraction) "
+        "split of the step's lines (qew_split_heights) is outside it: %.1f us per step, "
+        "timed alone" % (1e3 * ms_split / args.steps))
     results["fp32split"]["roofline"]["field_store"] = (
         "FP32 coefficients: 16 taps per edge" if args.no_edge_store else
         "FP32 coefficients plus the x-filtered copy: 4 taps per edge (the same rows, so the "
