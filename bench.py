@@ -93,6 +93,9 @@ def parse():
     ap.add_argument("--serve-rates", default="100,10000")
     ap.add_argument("--serve-requests", type=int, default=500)
     ap.add_argument("--serve-inflight", type=int, default=32)
+    ap.add_argument("--serve-lane-max", type=int, default=2048,
+                    help="static requests on lines of at most this many points go to the "
+                         "device-resident loop (0: none, at most 16384)")
     ap.add_argument("--serve-lsteps", type=int, default=10000)
     return ap.parse_args()
 
@@ -759,9 +762,12 @@ def run_serving(args, Q, torch):
            "request_counts": {name: int(sum(r["kind"] == kind for r in reqs))
                               for kind, name in ((0, "static"), (1, "langevin"),
                                                  (2, "depinning"))},
-           "static_on_device_loop": int(sum(r["kind"] == 0 and r["n"] < 2048 for r in reqs))}
+           "device_loop_limit": args.serve_lane_max,
+           "static_on_device_loop": int(sum(r["kind"] == 0 and r["n"] <= args.serve_lane_max
+                                            for r in reqs))}
     for rate in rates:
         srv = Q.Server(hbm_budget_bytes=150e9, max_inflight=args.serve_inflight)
+        srv.set_lane_limit(args.serve_lane_max)
         try:
             gaps = gaps_unit / rate
             t_next = srv.clock()

@@ -475,7 +475,8 @@ int qew_server_poll(qew_server *s, qew_response *out, int max);
 qew_status qew_server_drain(qew_server *s, double timeout_s);
 double qew_server_clock(const qew_server *s);
 /* The device-resident loop for static requests (no reference counterpart):
- * static requests on lines shorter than 2048 points at ftol 1e-8 are not
+ * static requests on lines of at most the lane limit (2048 points unless
+ * qew_server_set_lane_limit changes it) at ftol 1e-8 are not
  * given to a worker; a persistent grid (one CTA per SM) takes them from a
  * ring in mapped host memory as the host publishes them and relaxes each on
  * one CTA (FP32 phase, FP64 refinement, the ensemble's arithmetic), so they
@@ -486,6 +487,12 @@ double qew_server_clock(const qew_server *s);
  * when the loop could not be set up (all requests then go to workers). */
 qew_status qew_server_lane_stats(qew_server *s, uint64_t *served,
                                  uint64_t *launches);
+/* The lane limit: static requests on lines of at most max_n points (0: none,
+ * at most QEW_LANE_CAP_N) go to the device-resident loop from the next
+ * submission on. One CTA per line gives a long line alone a later result
+ * than a thread-block cluster, and many lines together more solves/s. */
+#define QEW_LANE_CAP_N 16384
+qew_status qew_server_set_lane_limit(qew_server *s, int max_n);
 qew_status qew_server_destroy(qew_server *s);
 
 /* --------------------------------------------------------------- Langevin */

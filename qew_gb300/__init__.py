@@ -1012,6 +1012,12 @@ class Server:
         return {"available": st == _capi.QEW_OK, "served": served.value,
                 "launches": launches.value}
 
+    def set_lane_limit(self, max_n: int) -> None:
+        """Static requests on lines of at most max_n points go to the
+        device-resident loop (qew_server_set_lane_limit; 0: none)."""
+        _capi.check(self.lib.qew_server_set_lane_limit(self.h, int(max_n)), None,
+                    "set_lane_limit")
+
     def drain(self, timeout_s: float = 600.0) -> None:
         _capi.check(self.lib.qew_server_drain(self.h, float(timeout_s)), None, "drain")
 

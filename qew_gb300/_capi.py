@@ -196,6 +196,7 @@ _SIGS = {
     "qew_server_create": (I, [I, D, I, C.POINTER(VP)]),
     "qew_server_submit": (I, [VP, C.POINTER(qew_request), C.POINTER(U64)]),
     "qew_server_lane_stats": (I, [VP, C.POINTER(U64), C.POINTER(U64)]),
+    "qew_server_set_lane_limit": (I, [VP, I]),
     "qew_server_poll": (I, [VP, C.POINTER(qew_response), I]),
     "qew_server_drain": (I, [VP, D]),
     "qew_server_clock": (D, [VP]),

@@ -53,6 +53,7 @@ struct qew_server {
     int workers_running = 0;  // requests the workers are serving
     int depinning_running = 0;  // of which depinning requests
     StaticLane *lane = nullptr;
+    int lane_max_n = 2048;
     std::thread lane_thread;
     uint64_t lane_served = 0;
     int running = 0;
@@ -66,15 +67,17 @@ struct qew_server {
 
 namespace {
 
-// Static requests on lines shorter than this (the length below which one CTA
-// per line beats a thread-block cluster), at the lane's tolerance, go to
-// the device-resident loop; the lane takes one persistent CTA per SM.
-constexpr int kLaneMaxN = 2048;
+// Static requests on lines of at most lane_max_n points (default 2048, the
+// length up to which one CTA per line beats a thread-block cluster for a
+// request alone; at most kLaneCapN, which sizes the loop's workspace), at
+// the lane's tolerance, go to the device-resident loop; the lane takes one
+// persistent CTA per SM.
+constexpr int kLaneCapN = QEW_LANE_CAP_N;
 constexpr double kLaneFtol = 1e-8;
 constexpr int kLaneWarpsPerSm = 16;
 
 bool lane_request(const qew_server *s, const qew_request &r) {
-    return s->lane && r.kind == QEW_REQ_STATIC && r.n < kLaneMaxN && r.ftol == kLaneFtol;
+    return s->lane && r.kind == QEW_REQ_STATIC && r.n <= s->lane_max_n && r.ftol == kLaneFtol;
 }
 
 // Device bytes a request holds at its peak: field generation (two FP64
@@ -469,7 +472,7 @@ qew_status qew_server_create(int device, double hbm_budget_bytes, int max_inflig
             lp.precondition = 1;
             lp.ls_fallback = 1;
             // the same settings as the worker path's static requests
-            if (qew_lane_create(device, kLaneMaxN, &lp, 2e-5, sms, &s->lane) != QEW_OK)
+            if (qew_lane_create(device, kLaneCapN, &lp, 2e-5, sms, &s->lane) != QEW_OK)
                 s->lane = nullptr;  // static requests then all take the worker path
         }
         cudaGetLastError();
@@ -502,6 +505,13 @@ qew_status qew_server_lane_stats(qew_server *s, uint64_t *served, uint64_t *laun
     if (served) *served = s->lane_served;
     if (launches) *launches = qew_lane_launches(s->lane);
     return s->lane ? QEW_OK : QEW_ERR_UNSUPPORTED;
+}
+
+qew_status qew_server_set_lane_limit(qew_server *s, int max_n) {
+    if (!s || max_n < 0 || max_n > kLaneCapN) return QEW_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->lane_max_n = max_n;
+    return QEW_OK;
 }
 
 qew_status qew_server_submit(qew_server *s, const qew_request *req, uint64_t *id) {

@@ -80,18 +80,27 @@ def test_budget_admission_and_limits(Q):
         with pytest.raises(ValueError):
             srv.submit(kind=2, n=512, rows=64, xi=4.0, seed=1, f_step=1e-12, f_max=40.0,
                        bisect_rtol=1e-3, max_sweeps=100)
+        # the device loop's workspace holds lines of at most 16384 points
+        for bad in (-1, 16385):
+            with pytest.raises(ValueError):
+                srv.set_lane_limit(bad)
     finally:
         srv.close()
 
 
-def test_static_lane_equals_ensemble(Q):
-    """Short static requests go to the device-resident loop; each result is
+@pytest.mark.parametrize("limit,specs", [
+    (None, [(512, 3.0, 21, 0), (1000, 2.5, 22, 1), (1536, 5.0, 23, 0), (2046, 4.0, 24, 1)]),
+    (16384, [(4096, 3.0, 25, 1), (9000, 6.0, 26, 0), (16384, 4.0, 27, 0)])])
+def test_static_lane_equals_ensemble(Q, limit, specs):
+    """Static requests up to the lane limit (2048 points by default, raised to
+    16384 here for long lines) go to the device-resident loop; each result is
     the one-line ensemble solve's (same field, same settings) bit for bit."""
     import torch
-    specs = [(512, 3.0, 21, 0), (1000, 2.5, 22, 1), (1536, 5.0, 23, 0), (2046, 4.0, 24, 1)]
     reqs = [dict(kind=0, n=n, rows=256, xi=xi, seed=sd, model=m, ftol=1e-8)
             for n, xi, sd, m in specs]
     srv = Q.Server(hbm_budget_bytes=20e9, max_inflight=2)
+    if limit is not None:
+        srv.set_lane_limit(limit)
     lines = [np.zeros(r["n"]) for r in reqs]
     try:
         ids = [srv.submit(h_out=lines[k], **r) for k, r in enumerate(reqs)]
