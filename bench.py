@@ -996,9 +996,12 @@ def run_ours(args):
     # DRAM bytes (read + write) per line point of each kernel from one ncu
     # capture of the bench's batched launch (8 lines of 2^20 points) on the
     # small field (each point touches the same number of rows whatever the
-    # field height), scaled to the points of one launch.
+    # field height), scaled to the points of one launch. k_gradient_poly: a
+    # warm launch inside the timed loop (--cache-control none); the others
+    # cold (ncu's cache flush, which leaves out the previous launch's
+    # write-back).
     dram_per_point = {
-        "k_gradient_poly": (342.742272e6 + 51.131904e6) / (8 * L_FULL),
+        "k_gradient_poly": (342.719232e6 + 69.857280e6) / (8 * L_FULL),
         "k_gradient_split_persist": (237.686784e6 + 22.566656e6) / (8 * L_FULL),
         "k_gradient_split": (241.858816e6 + 20.879104e6) / (8 * L_FULL),
         "k_gradient": (43.320832e6 + 0.039936e6) / L_FULL,
