@@ -856,7 +856,9 @@ def run_sections_only(args, Q, torch, rank):
         out[name] = runners[name](args, Q, torch)
         torch.cuda.empty_cache()
     if rank == 0:
-        print(json.dumps({"sections": out}), flush=True)
+        print(json.dumps({"sections": out,
+                          "autotune": [ln for ln in Q.tune_report().splitlines() if ln]}),
+              flush=True)
     return 0
 
 

@@ -609,9 +609,15 @@ qew_status qew_depinning_bisect_ex(qew_ctx *ctx, const qew_field *field,
  *                              a copy of the line advanced 24 sweeps; replaces
  *                              the warps-budget default only when more than
  *                              20 % faster)
+ *   3 QEW_TUNE_LANGEVIN_RUN    qew_langevin_run: one grid barrier per step, or
+ *                              K in {8,16,32} steps per barrier (temporal
+ *                              blocking) at {1,2,4} CTAs per SM (10; timed for
+ *                              64 steps of the run's schedule on a copy of the
+ *                              line, on runs of at least 4096 steps)
  * The shape class is the log2 of the work (points) and the kernel's variant
  * (model; noise form and GPU share for the sweeps). */
-enum { QEW_TUNE_GRADIENT_POLY = 0, QEW_TUNE_GRADIENT_SPLIT = 1, QEW_TUNE_RK_SEARCH = 2 };
+enum { QEW_TUNE_GRADIENT_POLY = 0, QEW_TUNE_GRADIENT_SPLIT = 1, QEW_TUNE_RK_SEARCH = 2,
+       QEW_TUNE_LANGEVIN_RUN = 3 };
 /* on = 0: this context uses the hand-chosen default shapes. */
 qew_status qew_ctx_set_autotune(qew_ctx *ctx, int on);
 /* Fixes kernel's candidate for this context (-1: tuned or default again). */

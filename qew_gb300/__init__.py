@@ -42,6 +42,7 @@ from ._capi import (QEW_FIELD_BSPLINE, QEW_FIELD_CONST, QEW_FIELD_HARMONIC,  # n
                     QEW_PREC_FP64, QEW_PREC_FP64_REFERENCE, QEW_RK_PLAIN, QEW_RK_RESIDENT,
                     QEW_STORE_FP32, QEW_STORE_FP32_EDGE, QEW_STORE_FP64, QEW_STORE_FP64_POLY,
                     QEW_TUNE_GRADIENT_POLY, QEW_TUNE_GRADIENT_SPLIT, QEW_TUNE_RK_SEARCH,
+                    QEW_TUNE_LANGEVIN_RUN,
                     QewError)
 
 __all__ = [

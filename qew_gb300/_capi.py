@@ -35,6 +35,7 @@ QEW_LBFGS_PLAIN, QEW_LBFGS_RESIDENT = 0, 1
 QEW_NOALLOC_MAX_N = 1048576
 QEW_RK_PLAIN, QEW_RK_RESIDENT = 0, 1
 QEW_TUNE_GRADIENT_POLY, QEW_TUNE_GRADIENT_SPLIT, QEW_TUNE_RK_SEARCH = 0, 1, 2
+QEW_TUNE_LANGEVIN_RUN = 3
 QEW_REQ_STATIC, QEW_REQ_LANGEVIN, QEW_REQ_DEPINNING = 0, 1, 2
 
 

@@ -47,7 +47,7 @@ struct qew_ctx {
     // launch-shape autotuning (qew_tune.cuh): on by default; tune_force[k]
     // >= 0 fixes kernel k's candidate (kernel ids of qew_tune.cuh)
     int autotune = 1;
-    int tune_force[3] = {-1, -1, -1};
+    int tune_force[4] = {-1, -1, -1, -1};
     std::string last_error;
     // copy streams and slot events of the host-buffer batch pipeline
     // (created on first use)

@@ -8,6 +8,7 @@
 // parity with the reference is checked through the increments entry point,
 // which takes xi from the caller.
 #include <algorithm>
+#include <climits>
 #include <new>
 #include <type_traits>
 #include <vector>
@@ -17,6 +18,7 @@
 #include "qew_model_kernels.cuh"
 #include "qew_noise32.cuh"
 #include "qew_philox.cuh"
+#include "qew_tune.cuh"
 
 struct qew_langevin {
     qew_ctx *ctx = nullptr;
@@ -146,6 +148,99 @@ k_langevin_run(Noise nz, double *h, double *tmp, int n, LineDx L, double lt, dou
         for (int i = blockIdx.x * kRunBS + t; i < n; i += gridDim.x * kRunBS) h[i] = __ldcg(cur + i);
 }
 
+// ---- the same run with K steps per grid barrier (temporal blocking) ----
+// CTA b owns the segment [b*seg, b*seg + S) of the ring (S = seg, shorter or
+// empty for the last CTAs). A round of Kr <= K steps loads the heights of
+// [s0 - Kr, s0 + S + Kr) (periodic) into shared memory and advances them
+// there: step s updates the positions s .. (region end - s) from step s - 1's
+// values, so the segment's heights after Kr steps are exactly those of Kr
+// single steps of the whole ring. Every position is computed as the one-step
+// kernel computes it (the same edge and site functions on the same operands,
+// the same increments: a site's Philox block is its global site pair's), so
+// the results are bitwise those of k_langevin_run; the halo positions are
+// computed by both neighbouring CTAs. One grid barrier per round.
+//
+// Shared memory, in doubles of the region R = seg + 2K: heights (two
+// buffers), edge values, arclength slopes, increments.
+constexpr int kTbBufs = 5;
+
+template <class Noise, bool NORMAL32>
+__global__ void __launch_bounds__(kRunBS)
+k_langevin_run_tb(Noise nz, double *h, double *tmp, int n, LineDx L, double lt, double f,
+                  int model, int steps, const double *__restrict__ drift,
+                  const double *__restrict__ diff, const unsigned long long *__restrict__ rstep,
+                  uint64_t seed, GridSync *sync, int seg, int K) {
+    extern __shared__ double s_tb[];
+    const int R = seg + 2 * K;
+    double *hA = s_tb, *hB = s_tb + R, *dv = s_tb + 2 * R, *sl = s_tb + 3 * R,
+           *zz = s_tb + 4 * R;
+    const bool arc = (model == QEW_MODEL_ARCLENGTH);
+    const int t = threadIdx.x;
+    const int s0 = blockIdx.x * seg;
+    const int S = max(0, min(seg, n - s0));
+    double *cur = h, *nxt = tmp;
+    for (int k0 = 0; k0 < steps; k0 += K) {
+        const int Kr = min(K, steps - k0);
+        if (S > 0) {
+            // local position r <-> global site (s0 - Kr + r) mod n, r in [0, S + 2 Kr)
+            int g0 = (s0 - Kr) % n;
+            if (g0 < 0) g0 += n;
+            auto gsite = [&](int r) {
+                int g = g0 + r;
+                if (g >= n) g -= n;
+                if (g >= n) g %= n;  // a ring shorter than the region
+                return g;
+            };
+            const int RS = S + 2 * Kr;
+            for (int r = t; r < RS; r += kRunBS) hA[r] = __ldcg(cur + gsite(r));
+            __syncthreads();
+            for (int s = 1; s <= Kr; ++s) {
+                const int k = k0 + s - 1;
+                const double a = drift[k], b = diff[k];
+                const uint64_t rs = rstep[k];
+                const int lo = s, hi = RS - s;  // positions updated at this step
+                for (int r = lo - 1 + t; r < hi; r += kRunBS)
+                    edge_gradient(nz, gsite(r), n, hA[r], hA[r + 1], L, arc, dv[r], sl[r]);
+                if (b > 0) {
+                    for (int r = lo + t; r < hi; r += kRunBS) {
+                        const int g = gsite(r);
+                        if ((g & 1) && r != lo) continue;  // its pair's first site wrote it
+                        double z0, z1;
+                        if (NORMAL32)
+                            philox_normal_pair_f32(seed, rs, (uint32_t)(g >> 1), z0, z1);
+                        else
+                            philox_normal_pair(seed, rs, (uint32_t)(g >> 1), z0, z1);
+                        zz[r] = (g & 1) ? z1 : z0;
+                        if (!(g & 1) && r + 1 < hi && g + 1 < n) zz[r + 1] = z1;
+                    }
+                }
+                __syncthreads();
+                for (int r = lo + t; r < hi; r += kRunBS) {
+                    const double gr = site_gradient(hA[r - 1], hA[r], hA[r + 1], dv[r - 1], dv[r],
+                                                    sl[r - 1], sl[r], L, lt, f, arc);
+                    hB[r] = (b > 0) ? hA[r] + (-a * gr + b * zz[r]) : hA[r] + -a * gr;
+                }
+                __syncthreads();
+                double *sw = hA;
+                hA = hB;
+                hB = sw;
+            }
+            for (int r = Kr + t; r < Kr + S; r += kRunBS) nxt[s0 + r - Kr] = hA[r];
+        }
+        if (!grid_sync_bounded(sync, gridDim.x)) return;
+        double *sw = cur;
+        cur = nxt;
+        nxt = sw;
+    }
+    if (cur != h)
+        for (int i = blockIdx.x * kRunBS + t; i < n; i += gridDim.x * kRunBS) h[i] = __ldcg(cur + i);
+}
+
+// Whether a functor gathers from the FP64 cell-polynomial store (a tuning class of its own).
+template <class Noise>
+bool reads_poly_store(const Noise &) { return false; }
+bool reads_poly_store(const NoiseBSpline64 &nz) { return nz.poly != nullptr; }
+
 qew_status check(qew_langevin *l, const qew_field *field, double *d_h, const qew_params *p) {
     if (!l || !l->ctx) return QEW_ERR_INVALID;
     if (!field || !d_h || !p)
@@ -244,39 +339,119 @@ qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h
         rs[k] = c;
         if (h_diff[k] > 0) ++c;
     }
+    const size_t vec = ((size_t)n * 8 + 255) & ~size_t(255);
     const size_t off_diff = ((size_t)steps * 8 + 255) & ~size_t(255);
     const size_t off_rs = off_diff + (((size_t)steps * 8 + 255) & ~size_t(255));
     const size_t off_tmp = off_rs + (((size_t)steps * 8 + 255) & ~size_t(255));
-    const size_t off_sync = off_tmp + (((size_t)n * 8 + 255) & ~size_t(255));
+    const size_t off_probe = off_tmp + vec;   // the tuning probe's line and its buffer
+    const size_t off_sync = off_probe + 2 * vec;
     QEW_TRY(qew_scratch_reserve(ctx, off_sync + sizeof(GridSync) + 256));
     char *base = (char *)ctx->scratch;
     double *d_drift = (double *)base, *d_diff = (double *)(base + off_diff);
     unsigned long long *d_rs = (unsigned long long *)(base + off_rs);
     double *tmp = (double *)(base + off_tmp);
+    double *probe_h = (double *)(base + off_probe), *probe_tmp = probe_h + vec / 8;
     GridSync *sync = (GridSync *)(base + off_sync);
     QEW_CUDA(ctx, cudaMemcpyAsync(d_drift, h_drift, (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
     QEW_CUDA(ctx, cudaMemcpyAsync(d_diff, h_diff, (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
     QEW_CUDA(ctx, cudaMemcpyAsync(d_rs, rs.data(), (size_t)steps * 8, cudaMemcpyHostToDevice, ctx->stream));
-    QEW_TRY(qew_gridsync_init(ctx, sync));
     LineDx L = make_line_dx(p->physical_size, n);
     double lt = p->line_tension, fd = p->driving_force;
     int model = p->model;
     uint64_t seed = l->seed;
+    int max_smem = 0;
+    QEW_CUDA(ctx, cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                                         ctx->device));
+    // Candidates (bitwise-equal results): 0 = one grid barrier per step
+    // (k_langevin_run); 1 + 3 i + j = temporal blocking at {1, 2, 4}[i] CTAs
+    // per SM and K = {8, 16, 32}[j] steps per barrier.
+    static const char *const names[10] = {
+        "1 step per barrier", "K=8 x 1 CTA/SM", "K=16 x 1 CTA/SM", "K=32 x 1 CTA/SM",
+        "K=8 x 2 CTA/SM", "K=16 x 2 CTA/SM", "K=32 x 2 CTA/SM", "K=8 x 4 CTA/SM",
+        "K=16 x 4 CTA/SM", "K=32 x 4 CTA/SM"};
     auto launch = [&](auto nz, auto normal32) -> qew_status {
-        auto kern = k_langevin_run<decltype(nz), decltype(normal32)::value>;
-        int per_sm = 0;
-        QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRunBS, 0));
-        const int want = (n + kRunTile - 1) / kRunTile;
-        int slots = ctx->num_sms * std::max(per_sm, 1);
-        if (ctx->warp_cap > 0) slots = std::min(slots, std::max(1, ctx->warp_cap / (kRunBS / 32)));
-        const int grid = std::max(1, std::min(want, slots));
-        void *args[] = {(void *)&nz, (void *)&d_h, (void *)&tmp, (void *)&n, (void *)&L,
-                        (void *)&lt, (void *)&fd, (void *)&model, (void *)&steps,
-                        (void *)&d_drift, (void *)&d_diff, (void *)&d_rs, (void *)&seed,
-                        (void *)&sync};
-        QEW_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kRunBS),
-                                                  args, 0, ctx->stream));
-        return qew_launch_check(ctx, "langevin_run");
+        constexpr bool kN32 = decltype(normal32)::value;
+        auto kern = k_langevin_run<decltype(nz), kN32>;
+        auto kern_tb = k_langevin_run_tb<decltype(nz), kN32>;
+        const int cap = ctx->warp_cap > 0 ? std::max(1, ctx->warp_cap / (kRunBS / 32)) : INT_MAX;
+        // grid, segment and shared memory of candidate c (c >= 1); false when
+        // its shared memory or co-residency does not fit
+        auto shape = [&](int c, int &grid, int &seg, int &K, size_t &smem) -> bool {
+            const int cps = 1 << ((c - 1) / 3);
+            K = 8 << ((c - 1) % 3);
+            grid = std::min(std::min(ctx->num_sms * cps, cap), std::max(1, n / 64));
+            seg = (n + grid - 1) / grid;
+            grid = (n + seg - 1) / seg;  // no empty CTAs
+            smem = (size_t)kTbBufs * (size_t)(seg + 2 * K) * sizeof(double);
+            if (smem > (size_t)max_smem) return false;
+            if (cudaFuncSetAttribute((const void *)kern_tb,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem) != cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            int per_sm = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern_tb, kRunBS, smem) !=
+                cudaSuccess) {
+                cudaGetLastError();
+                return false;
+            }
+            return grid <= per_sm * ctx->num_sms;
+        };
+        // candidate c on line hh (buffer tt) for nsteps steps of the schedule
+        auto run_on = [&](int c, double *hh, double *tt, int nsteps) -> qew_status {
+            QEW_TRY(qew_gridsync_init(ctx, sync));
+            int grid, seg, K;
+            size_t smem;
+            if (c >= 1 && shape(c, grid, seg, K, smem)) {
+                void *args[] = {(void *)&nz,     (void *)&hh,     (void *)&tt,     (void *)&n,
+                                (void *)&L,      (void *)&lt,     (void *)&fd,     (void *)&model,
+                                (void *)&nsteps, (void *)&d_drift, (void *)&d_diff, (void *)&d_rs,
+                                (void *)&seed,   (void *)&sync,   (void *)&seg,    (void *)&K};
+                QEW_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern_tb, dim3(grid),
+                                                          dim3(kRunBS), args, smem, ctx->stream));
+                return qew_launch_check(ctx, "langevin_run");
+            }
+            int per_sm = 0;
+            QEW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kRunBS, 0));
+            const int want = (n + kRunTile - 1) / kRunTile;
+            const int slots = std::min(ctx->num_sms * std::max(per_sm, 1), cap);
+            const int g1 = std::max(1, std::min(want, slots));
+            void *args[] = {(void *)&nz,     (void *)&hh,      (void *)&tt,     (void *)&n,
+                            (void *)&L,      (void *)&lt,      (void *)&fd,     (void *)&model,
+                            (void *)&nsteps, (void *)&d_drift, (void *)&d_diff, (void *)&d_rs,
+                            (void *)&seed,   (void *)&sync};
+            QEW_CUDA(ctx, cudaLaunchCooperativeKernel((const void *)kern, dim3(g1), dim3(kRunBS),
+                                                      args, 0, ctx->stream));
+            return qew_launch_check(ctx, "langevin_run");
+        };
+        // Runs of at least kTuneSteps steps time the candidates on a copy of
+        // the line (64 steps each, the schedule's first); shorter runs take a
+        // choice already made for their class, else the default.
+        constexpr int kTuneSteps = 4096, kProbeSteps = 64;
+        const int cls = qew_tune_class(n, (kN32 ? 1 : 0) + (model == QEW_MODEL_ARCLENGTH ? 2 : 0) +
+                                              (reads_poly_store(nz) ? 4 : 0));
+        // Default: one barrier per step. A blocked shape must be 5 % faster on
+        // the probe: where the FP64 work of a step (the FP64 Box-Muller
+        // increments above all) outweighs the barrier, the halo's extra work
+        // makes it slower.
+        const int dflt = 0;
+        int cand = dflt;
+        const int cached = qew_tune_cached(ctx->device, kTuneLangevinRun, cls);
+        if (ctx->tune_force[kTuneLangevinRun] >= 0 || (cached < 0 && steps >= kTuneSteps)) {
+            auto probe = [&](int c) -> qew_status {
+                QEW_CUDA(ctx, cudaMemcpyAsync(probe_h, d_h, (size_t)n * 8,
+                                              cudaMemcpyDeviceToDevice, ctx->stream));
+                return run_on(c, probe_h, probe_tmp, kProbeSteps);
+            };
+            QEW_TRY(qew_tune_pick(ctx, kTuneLangevinRun, cls, 10, dflt, names, probe, &cand,
+                                  0.05f));
+        } else if (cached >= 0 && ctx->autotune) {
+            cand = cached;
+        } else if (!ctx->autotune) {
+            cand = dflt;
+        }
+        return run_on(cand, d_h, tmp, steps);
     };
     if (precision == QEW_PREC_FP32_SPLIT) {
         if (field->kind != QEW_FIELD_BSPLINE || !field->coef32)

@@ -17,7 +17,7 @@ std::mutex g_mu;
 std::map<std::tuple<int, int, int>, Entry> g_cache;
 
 const char *kKernelNames[kTuneKernels] = {"k_gradient_poly", "k_gradient_split_persist",
-                                          "k_rk_resident"};
+                                          "k_rk_resident", "k_langevin_run"};
 
 }  // namespace
 

@@ -20,7 +20,8 @@ enum {
     kTuneGradientPoly = 0,   // k_gradient_poly: sites per thread x resident CTAs per SM
     kTuneGradientSplit = 1,  // k_gradient_split_persist: sites per thread x resident CTAs per SM
     kTuneRkSearch = 2,       // k_rk_resident: lanes per site's forward-zero search
-    kTuneKernels = 3
+    kTuneLangevinRun = 3,    // k_langevin_run / k_langevin_run_tb: steps per grid barrier x CTAs per SM
+    kTuneKernels = 4
 };
 
 // Shape class of a launch over `points` work items (log2 bucket) with a

@@ -108,3 +108,54 @@ def test_rk_search_candidates_bitwise_equal(Q, n):
         assert v == outs[0][1]
         assert torch.equal(h, outs[0][0])
     assert "k_rk_resident" in Q.tune_report()
+
+
+def _langevin_lines(Q, ctx, n, p, f, precision, steps=37, seed=3):
+    import torch
+    rng = np.random.default_rng(n)
+    h0 = 0.5 * f.Ly + 0.2 * rng.standard_normal(n) if hasattr(f, "Ly") else \
+        0.3 * rng.standard_normal(n)
+    drift = np.full(steps, 0.01)
+    diff = np.sqrt(2 * np.linspace(0.3, 0.05, steps) * 0.01)
+    diff[::5] = 0.0  # deterministic steps leave the Philox counter where it is
+
+    def run():
+        h = t64(h0)
+        d = Q.LangevinDynamics(n, seed, ctx=ctx)
+        d.run(h, p, f, drift, diff, precision=precision)
+        return h.clone(), d.steps
+    outs = _each_candidate(ctx, Q.QEW_TUNE_LANGEVIN_RUN, 10, run)
+    for c, (h, k) in enumerate(outs[1:], 1):
+        assert k == outs[0][1]
+        assert torch.equal(h.view(torch.int64), outs[0][0].view(torch.int64)), c
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_langevin_run_candidates_bitwise_equal(Q, model):
+    """One grid barrier per step or K in {8, 16, 32} steps per barrier at
+    1, 2 or 4 CTAs per SM: the same line, bit for bit, after 37 steps (the
+    last round partial), on the 16-tap FP64 gather, the cell-polynomial
+    store and the FP32 split gather."""
+    n, ny = 4096, 64
+    fld = gaussian_field(n, ny, 3.0, 40)
+    f16 = Q.FilteredNoise(fld, float(n), float(ny), store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP32)
+    fpoly = Q.FilteredNoise(fld, float(n), float(ny),
+                            store=Q.QEW_STORE_FP64 | Q.QEW_STORE_FP64_POLY)
+    ctx = f16.ctx
+    p = Q.Params(float(n), 1.1, 0.3, Q.Model(model))
+    _langevin_lines(Q, ctx, n, p, f16, Q.QEW_PREC_FP64)
+    _langevin_lines(Q, ctx, n, p, fpoly, Q.QEW_PREC_FP64)
+    _langevin_lines(Q, ctx, n, p, f16, Q.QEW_PREC_FP32_SPLIT)
+    # a line that is not one point per field column: the generic gather
+    f2 = Q.FilteredNoise(gaussian_field(1000, 48, 4.0, 41), 100.0, 4.8)
+    _langevin_lines(Q, ctx, 1000, Q.Params(100.0, 1.0, 0.2, Q.Model(model)), f2,
+                    Q.QEW_PREC_FP64)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 7, 130])
+def test_langevin_run_candidates_tiny_rings(Q, n):
+    """Rings shorter than a round's halo: the shared-memory region wraps the
+    ring several times and every copy of a site evolves alike."""
+    f = Q.SinusoidNoise(0.3, 1.7)
+    _langevin_lines(Q, f.ctx, n, Q.Params(float(n), 0.9, 0.1, Q.Model.Linear), f,
+                    Q.QEW_PREC_FP64)
