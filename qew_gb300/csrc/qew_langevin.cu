@@ -431,11 +431,13 @@ qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h
         constexpr int kTuneSteps = 4096, kProbeSteps = 64;
         const int cls = qew_tune_class(n, (kN32 ? 1 : 0) + (model == QEW_MODEL_ARCLENGTH ? 2 : 0) +
                                               (reads_poly_store(nz) ? 4 : 0));
-        // Default: one barrier per step. A blocked shape must be 5 % faster on
-        // the probe: where the FP64 work of a step (the FP64 Box-Muller
-        // increments above all) outweighs the barrier, the halo's extra work
-        // makes it slower.
-        const int dflt = 0;
+        // Defaults from measurement at L = 65536: FP32 runs K = 16 steps per
+        // barrier at 2 CTAs per SM (515 against 804 us per 64 steps); FP64
+        // runs one barrier per step, where the FP64 work of a step (the FP64
+        // Box-Muller increments above all) outweighs the barrier and the
+        // halo's extra work made the blocked shapes no faster. A tuned shape
+        // must be 5 % faster than the default on the probe.
+        const int dflt = kN32 ? 5 : 0;
         int cand = dflt;
         const int cached = qew_tune_cached(ctx->device, kTuneLangevinRun, cls);
         if (ctx->tune_force[kTuneLangevinRun] >= 0 || (cached < 0 && steps >= kTuneSteps)) {

@@ -246,6 +246,12 @@ void worker_main(qew_server *s) {
                     cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) == cudaSuccess;
     if (ok) {
         qew_ctx_set_stream(ctx, stream);
+        // Langevin runs keep one grid barrier per step in the workers, without
+        // tuning: a blocked run's cooperative grid, with its shared-memory
+        // regions, has to find room beside the other requests' kernels at
+        // launch, and a tuning probe times the other requests (the serving
+        // mix measured p50 26.9-36.8 s against 4.4 s at 100 req/s with them).
+        qew_ctx_force_tune_candidate(ctx, QEW_TUNE_LANGEVIN_RUN, 0);
     }
     // Persistent kernels of concurrent requests share the SMs: a request's
     // cooperative grids take at most its share of the GPU's warp slots (64 per
