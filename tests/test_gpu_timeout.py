@@ -24,26 +24,33 @@ def t64(a):
     return torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
 
 
-def test_langevin_run_barrier_times_out_then_recovers(Q):
+@pytest.mark.parametrize("cand", [0, 5])
+def test_langevin_run_barrier_times_out_then_recovers(Q, cand):
+    """One grid barrier per step (candidate 0: 32 CTAs of 256 sites) and 16
+    steps per barrier at 2 CTAs per SM (candidate 5: 128 CTAs of 64 sites)."""
     import torch
-    n, ny = 8192, 64  # 32 CTAs of 256 sites
+    n, ny = 8192, 64
     f = Q.FilteredNoise(gaussian_field(n, ny, 4.0, 3), float(n), float(ny))
     p = Q.Params(float(n), 1.0, 0.2, Q.Model.Arclength)
     drift, diff = np.full(50, 0.01), np.full(50, 0.05)
     h0 = t64(ny / 2 + np.random.default_rng(1).standard_normal(n))
     ctx = f.ctx
     try:
-        ctx.set_barrier_limits(SHORT, 3)
-        dyn = Q.LangevinDynamics(n, 7)
-        with pytest.raises(Q.QewError, match="timed out"):
-            dyn.run(h0.clone(), p, f, drift, diff)
+        ctx.force_tune_candidate(Q.QEW_TUNE_LANGEVIN_RUN, cand)
+        try:
+            ctx.set_barrier_limits(SHORT, 3)
+            dyn = Q.LangevinDynamics(n, 7)
+            with pytest.raises(Q.QewError, match="timed out"):
+                dyn.run(h0.clone(), p, f, drift, diff)
+        finally:
+            ctx.set_barrier_limits(0, -1)
+        # the same object and context afterwards: the run a fresh object gives
+        h1, h2 = h0.clone(), h0.clone()
+        dyn.run(h1, p, f, drift, diff)
+        Q.LangevinDynamics(n, 7).run(h2, p, f, drift, diff)
+        assert torch.equal(h1, h2)
     finally:
-        ctx.set_barrier_limits(0, -1)
-    # the same object and context afterwards: the run a fresh object gives
-    h1, h2 = h0.clone(), h0.clone()
-    dyn.run(h1, p, f, drift, diff)
-    Q.LangevinDynamics(n, 7).run(h2, p, f, drift, diff)
-    assert torch.equal(h1, h2)
+        ctx.force_tune_candidate(Q.QEW_TUNE_LANGEVIN_RUN, -1)
 
 
 def test_rk_block_barrier_times_out_then_recovers(Q):
