@@ -9,6 +9,7 @@
 // which takes xi from the caller.
 #include <algorithm>
 #include <climits>
+#include <mutex>
 #include <new>
 #include <type_traits>
 #include <vector>
@@ -384,11 +385,23 @@ qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h
             grid = (n + seg - 1) / seg;  // no empty CTAs
             smem = (size_t)kTbBufs * (size_t)(seg + 2 * K) * sizeof(double);
             if (smem > (size_t)max_smem) return false;
-            if (cudaFuncSetAttribute((const void *)kern_tb,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem) != cudaSuccess) {
-                cudaGetLastError();
-                return false;
+            // The kernel's dynamic shared-memory limit only ever rises (per
+            // device, under a lock), so a launch on another host thread never
+            // finds it lowered below its own size between set and launch.
+            {
+                static std::mutex mu;
+                static int raised[64] = {};
+                std::lock_guard<std::mutex> lock(mu);
+                const int d = ctx->device & 63;
+                if ((int)smem > raised[d]) {
+                    if (cudaFuncSetAttribute((const void *)kern_tb,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem) != cudaSuccess) {
+                        cudaGetLastError();
+                        return false;
+                    }
+                    raised[d] = (int)smem;
+                }
             }
             int per_sm = 0;
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern_tb, kRunBS, smem) !=
