@@ -164,6 +164,9 @@ k_langevin_run(Noise nz, double *h, double *tmp, int n, LineDx L, double lt, dou
 // Shared memory, in doubles of the region R = seg + 2K: heights (two
 // buffers), edge values, arclength slopes, increments.
 constexpr int kTbBufs = 5;
+// Dynamic shared memory a launch may take without raising the kernel's limit
+// (48 KB less room for the kernel's static shared memory).
+constexpr int kDefaultDynSmem = 47 * 1024;
 
 template <class Noise, bool NORMAL32>
 __global__ void __launch_bounds__(kRunBS)
@@ -385,22 +388,24 @@ qew_status qew_langevin_run(qew_langevin *l, const qew_field *field, double *d_h
             grid = (n + seg - 1) / seg;  // no empty CTAs
             smem = (size_t)kTbBufs * (size_t)(seg + 2 * K) * sizeof(double);
             if (smem > (size_t)max_smem) return false;
-            // The kernel's dynamic shared-memory limit only ever rises (per
-            // device, under a lock), so a launch on another host thread never
-            // finds it lowered below its own size between set and launch.
-            {
+            // Above the default 48 KB the kernel's dynamic shared-memory limit is
+            // raised to this shape's size, never lowered: under a lock, from the
+            // limit the device reports now (so a reset context is raised again),
+            // so a launch on another host thread never finds it below its own.
+            if (smem > (size_t)kDefaultDynSmem) {
                 static std::mutex mu;
-                static int raised[64] = {};
                 std::lock_guard<std::mutex> lock(mu);
-                const int d = ctx->device & 63;
-                if ((int)smem > raised[d]) {
-                    if (cudaFuncSetAttribute((const void *)kern_tb,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem) != cudaSuccess) {
-                        cudaGetLastError();
-                        return false;
-                    }
-                    raised[d] = (int)smem;
+                cudaFuncAttributes fa{};
+                if (cudaFuncGetAttributes(&fa, (const void *)kern_tb) != cudaSuccess) {
+                    cudaGetLastError();
+                    return false;
+                }
+                if (fa.maxDynamicSharedSizeBytes < (int)smem &&
+                    cudaFuncSetAttribute((const void *)kern_tb,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem) != cudaSuccess) {
+                    cudaGetLastError();
+                    return false;
                 }
             }
             int per_sm = 0;
